@@ -1,0 +1,236 @@
+"""ctypes binding of the scene/stepping facade.
+
+The product library exports the facade with the ``vx_`` prefix (``include/vx_capi.h``); test
+infrastructure exports the same function list under other prefixes, so :class:`Sim` takes the
+library path and the prefix.  Each method mirrors one call of the reference's public C++ API
+(``CVoxelyze`` in Voxelyze.h, ``CVX_Material`` in VX_Material.h, ``CVX_External`` in
+VX_External.h, ``CVX_Voxel`` in VX_Voxel.h) with the same argument meaning and error behaviour:
+setters return False where the reference returns false, ``do_time_step`` returns False on
+divergence (Voxelyze.cpp:265-269).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+# material property ids (VX_Material.h:75-107)
+PROP_POISSON, PROP_CTE, PROP_MU_STATIC, PROP_MU_KINETIC = 0, 1, 2, 3
+PROP_ZETA_INTERNAL, PROP_ZETA_GLOBAL, PROP_ZETA_COLLISION, PROP_DENSITY = 4, 5, 6, 7
+
+# dofComponent bits (VX_External.h:18-25)
+X_TRANSLATE, Y_TRANSLATE, Z_TRANSLATE = 1, 2, 4
+X_ROTATE, Y_ROTATE, Z_ROTATE = 8, 16, 32
+
+# stateInfoType / valueType (Voxelyze.h:48-67)
+(DISPLACEMENT, VELOCITY, KINETIC_ENERGY, ANGULAR_DISPLACEMENT, ANGULAR_VELOCITY, ENG_STRESS,
+ ENG_STRAIN, STRAIN_ENERGY, PRESSURE, MASS) = range(10)
+MIN, MAX, TOTAL, AVERAGE = range(4)
+
+_d = C.c_double
+_f = C.c_float
+_i = C.c_int
+_p = C.c_void_p
+_ip = C.POINTER(C.c_int)
+_fp = C.POINTER(C.c_float)
+_dp = C.POINTER(C.c_double)
+
+_SIGS = {
+    "create": (_p, [_d]),
+    "destroy": (None, [_p]),
+    "add_material": (_i, [_p, _f, _f]),
+    "material_set": (_i, [_p, _i, _i, _f]),
+    "material_set_model_linear": (_i, [_p, _i, _f, _f]),
+    "material_set_model_bilinear": (_i, [_p, _i, _f, _f, _f, _f]),
+    "material_set_model": (_i, [_p, _i, _i, _fp, _fp]),
+    "set_voxel": (_i, [_p, _i, _i, _i, _i]),
+    "set_voxels": (_i, [_p, _i, _ip, _ip]),
+    "voxel_count": (_i, [_p]),
+    "link_count": (_i, [_p]),
+    "voxel_index": (_i, [_p, _i, _i, _i]),
+    "external_set_fixed": (_i, [_p, _i, _i]),
+    "external_set_fixed_all": (_i, [_p, _i, _i]),
+    "external_set_displacement": (_i, [_p, _i, _i, _d]),
+    "external_set_displacement_all": (_i, [_p, _i, _dp, _dp]),
+    "external_clear_displacement": (_i, [_p, _i, _i]),
+    "external_set_force": (_i, [_p, _i, _f, _f, _f]),
+    "external_set_moment": (_i, [_p, _i, _f, _f, _f]),
+    "set_gravity": (None, [_p, _f]),
+    "enable_floor": (None, [_p, _i]),
+    "enable_collisions": (None, [_p, _i]),
+    "set_ambient_temperature": (None, [_p, _f, _i]),
+    "voxel_set_temperature": (_i, [_p, _i, _f]),
+    "do_time_step": (_i, [_p, _f]),
+    "do_time_steps": (_i, [_p, _i, _f]),
+    "recommended_time_step": (_f, [_p]),
+    "reset_time": (None, [_p]),
+    "current_time": (_f, [_p]),
+    "get_voxel_state": (_i, [_p, _dp, _fp, _ip]),
+    "get_link_state": (_i, [_p, _dp, _fp, _ip]),
+    "get_collisions": (_i, [_p, _ip, _i]),
+    "state_info": (_f, [_p, _i, _i]),
+}
+
+
+def bind(lib: C.CDLL, prefix: str) -> dict:
+    """Resolve every facade symbol ``<prefix>_<name>`` in ``lib`` and set its ctypes signature."""
+    fns = {}
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, f"{prefix}_{name}")
+        fn.restype = res
+        fn.argtypes = args
+        fns[name] = fn
+    return fns
+
+
+def _ptr(a: Optional[np.ndarray], ct):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ct))
+
+
+class Sim:
+    """One simulation instance (one ``CVoxelyze``) behind a facade library."""
+
+    def __init__(self, lib: C.CDLL, prefix: str, voxel_size: float = 0.001, fns: dict | None = None):
+        self.lib = lib
+        self.prefix = prefix
+        self.f = fns if fns is not None else bind(lib, prefix)
+        self.h = self.f["create"](voxel_size)
+        if not self.h:
+            raise RuntimeError(f"{prefix}_create failed")
+
+    def close(self):
+        if self.h:
+            self.f["destroy"](self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- materials -------------------------------------------------------------------------
+    def add_material(self, E: float = 1e6, rho: float = 1e3) -> int:
+        return self.f["add_material"](self.h, E, rho)
+
+    def material_set(self, mat: int, prop: int, value: float) -> bool:
+        return self.f["material_set"](self.h, mat, prop, value) == 0
+
+    def set_model_linear(self, mat, E, fail=-1.0) -> bool:
+        return self.f["material_set_model_linear"](self.h, mat, E, fail) == 0
+
+    def set_model_bilinear(self, mat, E, plastic_E, yield_stress, fail=-1.0) -> bool:
+        return self.f["material_set_model_bilinear"](self.h, mat, E, plastic_E, yield_stress, fail) == 0
+
+    def set_model(self, mat, strain, stress) -> bool:
+        a = np.ascontiguousarray(strain, dtype=np.float32)
+        b = np.ascontiguousarray(stress, dtype=np.float32)
+        return self.f["material_set_model"](self.h, mat, len(a), _ptr(a, C.c_float), _ptr(b, C.c_float)) == 0
+
+    # -- voxels ----------------------------------------------------------------------------
+    def set_voxel(self, mat: int, x: int, y: int, z: int) -> int:
+        return self.f["set_voxel"](self.h, mat, x, y, z)
+
+    def set_voxels(self, mats: np.ndarray, xyz: np.ndarray) -> None:
+        m = np.ascontiguousarray(mats, dtype=np.int32)
+        p = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1)
+        self.f["set_voxels"](self.h, len(m), _ptr(m, C.c_int), _ptr(p, C.c_int))
+
+    def voxel_count(self) -> int:
+        return self.f["voxel_count"](self.h)
+
+    def link_count(self) -> int:
+        return self.f["link_count"](self.h)
+
+    def voxel_index(self, x, y, z) -> int:
+        return self.f["voxel_index"](self.h, x, y, z)
+
+    # -- externals -------------------------------------------------------------------------
+    def set_fixed(self, v, mask: int):
+        self.f["external_set_fixed"](self.h, v, mask)
+
+    def set_fixed_all(self, v, fixed=True):
+        self.f["external_set_fixed_all"](self.h, v, 1 if fixed else 0)
+
+    def set_displacement(self, v, dof: int, value: float = 0.0):
+        self.f["external_set_displacement"](self.h, v, dof, value)
+
+    def set_displacement_all(self, v, translation=(0.0, 0.0, 0.0), rotation=(0.0, 0.0, 0.0)):
+        t = np.ascontiguousarray(translation, dtype=np.float64)
+        r = np.ascontiguousarray(rotation, dtype=np.float64)
+        self.f["external_set_displacement_all"](self.h, v, _ptr(t, C.c_double), _ptr(r, C.c_double))
+
+    def clear_displacement(self, v, dof: int):
+        self.f["external_clear_displacement"](self.h, v, dof)
+
+    def set_force(self, v, fx, fy, fz):
+        self.f["external_set_force"](self.h, v, fx, fy, fz)
+
+    def set_moment(self, v, mx, my, mz):
+        self.f["external_set_moment"](self.h, v, mx, my, mz)
+
+    # -- globals ---------------------------------------------------------------------------
+    def set_gravity(self, g: float = 1.0):
+        self.f["set_gravity"](self.h, g)
+
+    def enable_floor(self, on=True):
+        self.f["enable_floor"](self.h, 1 if on else 0)
+
+    def enable_collisions(self, on=True):
+        self.f["enable_collisions"](self.h, 1 if on else 0)
+
+    def set_ambient_temperature(self, t: float, all_voxels: bool = False):
+        self.f["set_ambient_temperature"](self.h, t, 1 if all_voxels else 0)
+
+    def set_temperature(self, v: int, t: float):
+        self.f["voxel_set_temperature"](self.h, v, t)
+
+    # -- stepping --------------------------------------------------------------------------
+    def do_time_step(self, dt: float = -1.0) -> bool:
+        return self.f["do_time_step"](self.h, dt) == 1
+
+    def do_time_steps(self, n: int, dt: float = -1.0) -> int:
+        return self.f["do_time_steps"](self.h, n, dt)
+
+    def recommended_time_step(self) -> float:
+        return self.f["recommended_time_step"](self.h)
+
+    def reset_time(self):
+        self.f["reset_time"](self.h)
+
+    def current_time(self) -> float:
+        return self.f["current_time"](self.h)
+
+    def state_info(self, info: int, vtype: int) -> float:
+        return self.f["state_info"](self.h, info, vtype)
+
+    # -- readback --------------------------------------------------------------------------
+    def voxel_state(self) -> dict:
+        n = self.voxel_count()
+        d = np.zeros((n, 13), np.float64)
+        f = np.zeros((n, 5), np.float32)
+        i = np.zeros((n, 2), np.int32)
+        self.f["get_voxel_state"](self.h, _ptr(d, C.c_double), _ptr(f, C.c_float), _ptr(i, C.c_int))
+        return {"pos": d[:, 0:3], "linMom": d[:, 3:6], "orient": d[:, 6:10], "angMom": d[:, 10:13],
+                "temp": f[:, 0], "previousDt": f[:, 1], "pStrain": f[:, 2:5],
+                "staticFriction": i[:, 0], "pStrainInvalid": i[:, 1], "raw_d": d, "raw_f": f, "raw_i": i}
+
+    def link_state(self) -> dict:
+        n = self.link_count()
+        d = np.zeros((n, 22), np.float64)
+        f = np.zeros((n, 6), np.float32)
+        i = np.zeros((n, 6), np.int32)
+        self.f["get_link_state"](self.h, _ptr(d, C.c_double), _ptr(f, C.c_float), _ptr(i, C.c_int))
+        return {"pos2": d[:, 0:3], "angle1v": d[:, 3:6], "angle2v": d[:, 6:9], "forceNeg": d[:, 9:12],
+                "forcePos": d[:, 12:15], "momentNeg": d[:, 15:18], "momentPos": d[:, 18:21],
+                "restLength": d[:, 21], "strain": f[:, 0], "maxStrain": f[:, 1], "strainOffset": f[:, 2],
+                "stress": f[:, 3], "transverseArea": f[:, 4], "transverseStrainSum": f[:, 5],
+                "smallAngle": i[:, 0], "localVelValid": i[:, 1], "axis": i[:, 2], "vneg": i[:, 3],
+                "vpos": i[:, 4], "mat": i[:, 5], "raw_d": d, "raw_f": f, "raw_i": i}
+
+    def collisions(self) -> np.ndarray:
+        n = self.f["get_collisions"](self.h, None, 0)
+        out = np.zeros((max(n, 1), 2), np.int32)
+        self.f["get_collisions"](self.h, _ptr(out, C.c_int), n)
+        return out[:n]
