@@ -1,0 +1,63 @@
+/* vx_capi — C facade of the drop-in CVoxelyze API, for callers that bind C symbols (ctypes, cgo,
+ * JNI, N-API).  Each call wraps one call of the C++ API with the same argument meaning and error
+ * behaviour; the reference interface it mirrors is cited beside it (file:line in the reference
+ * tree).  Objects are addressed by index: materials in creation order, voxels in voxel-list order.
+ * Calls returning int give 0 (or an index / count) on success and -1 on a bad argument.
+ */
+#ifndef VX_CAPI_H
+#define VX_CAPI_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+void* vx_create(double voxel_size);                         /* CVoxelyze(double)        src/Voxelyze.cpp:28-32 */
+void vx_destroy(void* s);                                   /* ~CVoxelyze               src/Voxelyze.cpp:34-37 */
+int vx_add_material(void* s, float E, float rho);           /* addMaterial(float,float) src/Voxelyze.cpp:357-366 */
+int vx_material_set(void* s, int mat, int prop, float value); /* CVX_Material::set*     src/VX_Material.cpp:472-515 */
+int vx_material_set_model_linear(void* s, int mat, float E, float fail_stress);   /* src/VX_Material.cpp:355-384 */
+int vx_material_set_model_bilinear(void* s, int mat, float E, float plastic_E, float yield_stress,
+                                   float fail_stress);                            /* src/VX_Material.cpp:389-434 */
+int vx_material_set_model(void* s, int mat, int n, const float* strain, const float* stress); /* :283-350 */
+int vx_set_voxel(void* s, int mat, int x, int y, int z);    /* setVoxel                 src/Voxelyze.cpp:422-437 */
+int vx_set_voxels(void* s, int n, const int* mat, const int* xyz); /* n setVoxel calls in order */
+int vx_voxel_count(void* s);                                /* voxelCount               include/Voxelyze.h:98 */
+int vx_link_count(void* s);                                 /* linkCount                include/Voxelyze.h:111 */
+int vx_voxel_index(void* s, int x, int y, int z);           /* voxel(x,y,z) -> index or -1 */
+int vx_external_set_fixed(void* s, int v, int dof_mask);    /* CVX_External::setFixed(6 bools) src/VX_External.cpp:47-51 */
+int vx_external_set_fixed_all(void* s, int v, int fixed);   /* setFixedAll              include/VX_External.h:60 */
+int vx_external_set_displacement(void* s, int v, int dof, double value); /* src/VX_External.cpp:53-66 */
+int vx_external_set_displacement_all(void* s, int v, const double* t3, const double* r3); /* :68-75 */
+int vx_external_clear_displacement(void* s, int v, int dof); /* src/VX_External.cpp:77-89 */
+int vx_external_set_force(void* s, int v, float fx, float fy, float fz);  /* include/VX_External.h:69 */
+int vx_external_set_moment(void* s, int v, float mx, float my, float mz); /* include/VX_External.h:71 */
+void vx_set_gravity(void* s, float g);                      /* src/Voxelyze.cpp:596-602 */
+void vx_enable_floor(void* s, int enabled);                 /* src/Voxelyze.cpp:604-610 */
+void vx_enable_collisions(void* s, int enabled);            /* src/Voxelyze.cpp:612-622 */
+void vx_set_ambient_temperature(void* s, float t, int all_voxels); /* src/Voxelyze.cpp:585-594 */
+int vx_voxel_set_temperature(void* s, int v, float t);      /* CVX_Voxel::setTemperature src/VX_Voxel.cpp:108-114 */
+int vx_do_time_step(void* s, float dt);                     /* doTimeStep: 1 ok, 0 diverged, -1 error  src/Voxelyze.cpp:251-284 */
+int vx_do_time_steps(void* s, int n, float dt);             /* n doTimeStep calls in one GPU batch; steps completed */
+float vx_recommended_time_step(void* s);                    /* src/Voxelyze.cpp:286-311 */
+void vx_reset_time(void* s);                                /* src/Voxelyze.cpp:313-321 */
+float vx_current_time(void* s);                             /* CVoxelyze::currentTime   include/Voxelyze.h:138 */
+/* full state dumps, layouts as in oracle/facade.h: voxels d13/f5/i2, links d22/f6/i6 */
+int vx_get_voxel_state(void* s, double* d13, float* f5, int* i2);
+int vx_get_link_state(void* s, double* d22, float* f6, int* i6);
+int vx_get_collisions(void* s, int* pairs, int cap);        /* collisionList() as index pairs */
+float vx_state_info(void* s, int info, int type);           /* stateInfo                src/Voxelyze.cpp:752-800 */
+
+/* extensions for throughput users */
+int vx_set_precision(void* s, int mode);                    /* 0 = FP64 (default), 1 = FP32C */
+int vx_read_positions(void* s, double* xyz);                /* 3 n_voxels doubles, component-major, straight from the GPU */
+int vx_set_temperatures(void* s, const float* t);           /* n_voxels floats: every voxel's setTemperature */
+float vx_state_info_device(void* s, int info, int type);    /* GPU reduction, see vxg_reduce */
+int vx_counters(void* s, long long* out, int n);            /* vxg_counters of the engine */
+int vx_enable_timing(void* s, int on);                      /* vxg_enable_timing */
+int vx_step_timing(void* s, float* out4);                   /* batch ms, link/collide/voxel ms per step */
+const char* vx_last_error(void* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,183 @@
+/* vxg — C ABI of the GB300 time-step engine (sm_103a).
+ *
+ * The drop-in C++ API (Voxelyze.h and friends) builds the scene on the host in the reference's
+ * voxel and link order and drives the engine through these calls only.  Everything crossing the
+ * boundary is a plain pointer plus a count; device memory never leaves the engine.  All calls
+ * return 0 on success and a negative VXG_E* code otherwise; they never abort.  One engine is
+ * driven by one host thread (the reference is not thread-safe either, Voxelyze.h:134).
+ *
+ * Reference interfaces these calls replace (file:line in the reference tree):
+ *   vxg_step            CVoxelyze::doTimeStep                      src/Voxelyze.cpp:251-284
+ *                         link pass  CVX_Link::updateForces         src/VX_Link.cpp:149-217
+ *                         collisions CVoxelyze::updateCollisions    src/Voxelyze.cpp:670-710
+ *                         voxel pass CVX_Voxel::timeStep            src/VX_Voxel.cpp:162-232
+ *   vxg_recommended_dt  CVoxelyze::recommendedTimeStep             src/Voxelyze.cpp:286-311
+ *   vxg_set_all_temperatures  CVoxelyze::setAmbientTemperature(t, true)  src/Voxelyze.cpp:585-594
+ *   vxg_reduce          CVoxelyze::stateInfo                       src/Voxelyze.cpp:752-800
+ *   vxg_set_field / vxg_get_field  the voxel and link state members  include/VX_Voxel.h:150-192,
+ *                                                                    include/VX_Link.h:70-107
+ */
+#ifndef VXG_H
+#define VXG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct vxg_engine vxg_engine;
+
+/* precision modes */
+enum { VXG_FP64 = 0,   /* bit-faithful to the reference's double-precision arithmetic */
+       VXG_FP32C = 1   /* FP32 bulk arithmetic, lattice origin + compensated FP32 displacement */ };
+
+/* error codes */
+enum { VXG_OK = 0, VXG_E_ARG = -1, VXG_E_CUDA = -2, VXG_E_STATE = -3, VXG_E_SIZE = -4,
+       VXG_E_DEVICE_STATUS = -5 };
+
+#define VXG_MAX_MODEL_POINTS 32
+
+/* voxel flag bits (per voxel, uint32) */
+enum { VXG_VF_FLOOR = 1, VXG_VF_STATIC_FRICTION = 2, VXG_VF_COLLISIONS = 4, VXG_VF_INTERIOR = 8,
+       VXG_VF_PSTRAIN_INVALID = 16 };
+/* link flag bits (per link, uint32); bits 8..9 hold the axis */
+enum { VXG_LF_SMALL_ANGLE = 1, VXG_LF_LOCAL_VEL_VALID = 2 };
+
+/* Voxel material constants, all derived on the host exactly as CVX_MaterialVoxel::updateDerived
+ * (src/VX_MaterialVoxel.cpp:57-79) and CVX_Material (include/VX_Material.h:117-140). */
+typedef struct {
+  float E, nu, rho, alphaCTE, muStatic, muKinetic, zetaInternal, zetaGlobal, zetaCollision;
+  float mass, massInv, sqrtMass, inertia, inertiaInv, c2xSqMxExS, c2xSqIxExSxSxS;
+  float gravMult, penetrationStiffness, eHat, pad0;
+  double nomSize;
+  double size[3];  /* nomSize * external scale factor per axis (CVX_MaterialVoxel::size) */
+  int powf_slot;   /* powf table slot for exponent -nu, -1 when nu == 0 */
+  int pad1;
+} vxg_voxel_material;
+
+/* Link material constants (src/VX_MaterialLink.cpp:45-141) with its stress-strain model data. */
+typedef struct {
+  int linear, ndata;
+  float E, nu, eHat, epsilonFail;
+  float a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp;
+  float strain[VXG_MAX_MODEL_POINTS], stress[VXG_MAX_MODEL_POINTS];
+} vxg_link_material;
+
+/* One voxel's externals (include/VX_External.h:92-97).  rotq is the cached quaternion the
+ * reference keeps in _extRotationQ (identity unless a rotation was prescribed). */
+typedef struct {
+  int dof; /* dofComponent bits */
+  float force[3], moment[3];
+  int pad;
+  double translation[3];
+  double rotq[4];
+} vxg_external;
+
+typedef struct {
+  int collisions;          /* CVoxelyze collisions flag */
+  int any_poisson;         /* some voxel material has nu != 0 */
+  float boundingRadius;    /* Voxelyze.cpp:353 */
+  float watchDistance;     /* Voxelyze.cpp:354 */
+  double voxSize;
+  float fallback_freq2;    /* recommendedTimeStep's per-voxel E*L/m maximum, used when no link has one */
+  int pad;
+} vxg_globals;
+
+/* State and topology fields for vxg_set_field / vxg_get_field.  Multi-component fields are
+ * component-major: all x, then all y, ...  Counts are in elements. */
+enum {
+  /* voxel topology */
+  VXG_F_VOXEL_MATERIAL = 0, /* int32  [n_voxels] */
+  VXG_F_VOXEL_INDEX,        /* int32  [3 n_voxels] lattice ix, iy, iz */
+  VXG_F_VOXEL_LINKS,        /* int32  [6 n_voxels] link per direction X+,X-,Y+,Y-,Z+,Z- or -1 */
+  VXG_F_VOXEL_EXTERNAL,     /* int32  [n_voxels] external slot or -1 */
+  /* voxel state */
+  VXG_F_POS,                /* double [3 n_voxels] */
+  VXG_F_LINMOM,             /* double [3 n_voxels] */
+  VXG_F_ORIENT,             /* double [4 n_voxels] w, x, y, z */
+  VXG_F_ANGMOM,             /* double [3 n_voxels] */
+  VXG_F_TEMP,               /* float  [n_voxels] */
+  VXG_F_PREV_DT,            /* float  [n_voxels] */
+  VXG_F_PSTRAIN,            /* float  [3 n_voxels] cached Poisson strain */
+  VXG_F_VOXEL_FLAGS,        /* uint32 [n_voxels] VXG_VF_* */
+  /* link topology */
+  VXG_F_LINK_VOXELS,        /* int32  [2 n_links] negative end, positive end */
+  VXG_F_LINK_MATERIAL,      /* int32  [n_links] */
+  /* link state */
+  VXG_F_LINK_FLAGS,         /* uint32 [n_links] VXG_LF_* | axis << 8 */
+  VXG_F_POS2,               /* double [3 n_links] */
+  VXG_F_ANGLE1V,            /* double [3 n_links] */
+  VXG_F_ANGLE2V,            /* double [3 n_links] */
+  VXG_F_FORCE_NEG,          /* double [3 n_links] */
+  VXG_F_FORCE_POS,          /* double [3 n_links] */
+  VXG_F_MOMENT_NEG,         /* double [3 n_links] */
+  VXG_F_MOMENT_POS,         /* double [3 n_links] */
+  VXG_F_REST_LENGTH,        /* double [n_links] */
+  VXG_F_STRAIN,             /* float  [n_links] */
+  VXG_F_MAX_STRAIN,         /* float  [n_links] */
+  VXG_F_STRAIN_OFFSET,      /* float  [n_links] */
+  VXG_F_STRESS,             /* float  [n_links] */
+  VXG_F_STRAIN_RATIO,       /* float  [n_links] */
+  VXG_F_TRANSVERSE_AREA,    /* float  [n_links] */
+  VXG_F_TRANSVERSE_STRAIN_SUM, /* float [n_links] */
+  /* scalars */
+  VXG_F_TIME,               /* float  [1] CVoxelyze::currentTime */
+  VXG_F_COUNT
+};
+
+/* counters returned by vxg_counters */
+enum { VXG_C_TRANSCENDENTAL = 0, /* correctly rounded sin/cos/acos evaluations */
+       VXG_C_AMBIGUOUS = 1,      /* evaluations whose rounding could not be certified */
+       VXG_C_LIBM_BAND = 2,      /* evaluations within 1/64 ulp of a rounding midpoint */
+       VXG_C_POWF_MISS = 3,      /* powf arguments outside the tabulated range */
+       VXG_C_REBUILDS = 4,       /* collision pair-list rebuilds */
+       VXG_C_PAIRS = 5,          /* current number of collision pairs */
+       VXG_C_COUNT = 8 };
+
+int vxg_create(vxg_engine** out, int device, int precision);
+int vxg_destroy(vxg_engine* e);
+int vxg_precision(const vxg_engine* e);
+/* (Re)allocates every device array for the given counts.  State is undefined until set. */
+int vxg_resize(vxg_engine* e, int n_voxels, int n_links);
+int vxg_set_field(vxg_engine* e, int field, const void* host, long long count);
+int vxg_get_field(vxg_engine* e, int field, void* host, long long count);
+int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const vxg_link_material* lm,
+                   int n_lm, const vxg_external* ext, int n_ext);
+/* Tabulated powf(x, exponent) for every float x in [0.5, 2): 2^24 entries indexed by
+ * (bits(x) - bits(0.5f)), computed on the host by the C library the reference links. */
+int vxg_set_powf_table(vxg_engine* e, int slot, float exponent, const float* table);
+int vxg_set_globals(vxg_engine* e, const vxg_globals* g);
+/* Collision lattice data: per voxel, the sorted list of surface voxels within 5 link hops
+ * (CVX_Voxel::generateNearby, src/VX_Voxel.cpp:395-418), CSR form. */
+int vxg_set_nearby(vxg_engine* e, const int* offsets /* n_voxels+1 */, const int* items, long long n_items);
+/* Runs nsteps of doTimeStep(dt); dt < 0 recomputes recommendedTimeStep every step.  Stops at the
+ * first divergent step like the reference (links advanced, voxels not).  *steps_done receives the
+ * number of completed steps, *diverged 1 if the run stopped on divergence. */
+int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged);
+/* recommendedTimeStep() with its side effects on link state when nu != 0. */
+int vxg_recommended_dt(vxg_engine* e, float* dt);
+int vxg_set_all_temperatures(vxg_engine* e, float t);
+/* Every voxel's CVX_Voxel::setTemperature at once (n_voxels floats), then every rest length. */
+int vxg_set_temperatures(vxg_engine* e, const float* t);
+/* stateInfo(info, type).  MIN/MAX are exact; TOTAL/AVERAGE accumulate in double. */
+int vxg_reduce(vxg_engine* e, int info, int type, float* out);
+/* Collision pairs in the reference's order (i < j, voxel-list order), 2 ints per pair.
+ * Returns the pair count through *n (pairs beyond cap are not written). */
+int vxg_get_collisions(vxg_engine* e, int* pairs, int cap, int* n);
+int vxg_counters(vxg_engine* e, long long* out, int n);
+/* Timing mode: vxg_step records CUDA events on the engine stream around the link pass (with the
+ * Poisson pre-pass), the collision stage and the voxel pass of every step (no graph replay).
+ * vxg_last_step_timing gives the per-step averages of the last batch in milliseconds,
+ * vxg_last_batch_ms the device time from its first to its last kernel. */
+int vxg_enable_timing(vxg_engine* e, int on);
+int vxg_last_step_timing(vxg_engine* e, float* ms_link, float* ms_collide, float* ms_voxel);
+int vxg_last_batch_ms(vxg_engine* e, float* ms);
+const char* vxg_last_error(const vxg_engine* e);
+void* vxg_stream(vxg_engine* e); /* cudaStream_t the engine launches on */
+int vxg_synchronize(vxg_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

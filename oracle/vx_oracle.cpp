@@ -24,8 +24,28 @@
 #include <vector>
 
 #include "facade.h"
+// Correctly rounded sin/cos/acos, selectable with vxo_set_math(1).  The GPU path evaluates these
+// functions correctly rounded; the C library the reference links is not correctly rounded in about
+// 0.1% of calls.  In mode 1 the oracle uses the same correctly rounded values (validated on their
+// own against 256-bit arithmetic in tests/test_crmath.py), so GPU parity can be checked bit for bit;
+// mode 0 (default) is the faithful restatement of the reference with the C library.
+#include "vx_crmath.h"
 
 namespace vxo {
+
+static int g_math_mode = 0;
+static inline double m_sin(double x) {
+  if (g_math_mode) { int f = 0; return vxm::cr_sin(x, &f); }
+  return std::sin(x);
+}
+static inline double m_cos(double x) {
+  if (g_math_mode) { int f = 0; return vxm::cr_cos(x, &f); }
+  return std::cos(x);
+}
+static inline double m_acos(double x) {
+  if (g_math_mode) { int f = 0; return vxm::cr_acos(x, &f); }
+  return std::acos(x);
+}
 
 // ---------------------------------------------------------------------------------------------
 // small vector / quaternion helpers (Vec3D.h, Quat3D.h semantics)
@@ -74,7 +94,7 @@ static inline V3 to_rotation_vector(const Q4& q) {
     double s = std::sqrt((2 - 2 * q.w) / sl);
     return v3(s * (2.0 * q.x), s * (2.0 * q.y), s * (2.0 * q.z));
   }
-  double a = std::acos(q.w);
+  double a = m_acos(q.w);
   double inv = 1.0 / std::sqrt(sl);
   return v3(inv * (a * (2.0 * q.x)), inv * (a * (2.0 * q.y)), inv * (a * (2.0 * q.z)));
 }
@@ -88,8 +108,8 @@ static inline Q4 from_rotation_vector(const V3& in) {
     s = 1.0 - m2 / 6.0;
   } else {
     double m = std::sqrt(m2);
-    w = std::cos(m);
-    s = std::sin(m) / m;
+    w = m_cos(m);
+    s = m_sin(m) / m;
   }
   return q4(w, th.x * s, th.y * s, th.z * s);
 }
@@ -110,15 +130,15 @@ static inline void from_angle_to_pos_x(Q4& q, const V3& r) {
     double li = 1.0 / l;
     n.x *= li; n.y *= li; n.z *= li;
   }
-  double theta = std::acos(n.x);
+  double theta = m_acos(n.x);
   if (theta > 3.14159265358979 - 1e-7) {
     q = q4(0, 0, 1, 0);
     return;
   }
   double ami = 1.0 / std::sqrt(n.z * n.z + n.y * n.y);
   double a = 0.5 * theta;
-  double s = std::sin(a);
-  q.w = std::cos(a);
+  double s = m_sin(a);
+  q.w = m_cos(a);
   q.x = 0;
   q.y = n.z * ami * s;
   q.z = -n.y * ami * s;
@@ -1178,6 +1198,19 @@ void vxo_destroy(void* s) { delete S(s); }
 
 // CPU threads for the link and voxel loops (the reference's USE_OMP build); 1 = serial.
 void vxo_set_threads(void* s, int n) { S(s)->nthreads = n < 1 ? 1 : n; }
+
+// 0: sin/cos/acos from the C library (the reference's arithmetic); 1: correctly rounded.
+void vxo_set_math(int mode) { vxo::g_math_mode = mode ? 1 : 0; }
+
+// Evaluates the correctly rounded functions of vx_crmath.h on the host (fn 0 sin, 1 cos, 2 acos)
+// so tests can check them against high-precision arithmetic.
+void vxo_crmath_eval(int fn, int n, const double* x, double* y, int* flags) {
+  for (int i = 0; i < n; ++i) {
+    int f = 0;
+    y[i] = fn == 0 ? vxm::cr_sin(x[i], &f) : (fn == 1 ? vxm::cr_cos(x[i], &f) : vxm::cr_acos(x[i], &f));
+    if (flags) flags[i] = f;
+  }
+}
 
 int vxo_add_material(void* s, float E, float rho) {  // Voxelyze.cpp:357-366
   Sim* r = S(s);

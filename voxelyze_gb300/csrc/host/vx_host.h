@@ -1,0 +1,84 @@
+// Private host-side state of a CVoxelyze: the structure-of-arrays mirror of the GPU state (in the
+// reference's voxel-list and link-list order), the dirty flags that decide what to upload before
+// the next step, and the engine handle.
+#pragma once
+#include <cstdint>
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "vxg.h"
+
+class CVoxelyze;
+class CVX_Voxel;
+class CVX_Link;
+
+// voxel doubles / floats and link doubles / floats of the mirror
+enum { VD_PX, VD_PY, VD_PZ, VD_LX, VD_LY, VD_LZ, VD_OW, VD_OX, VD_OY, VD_OZ, VD_AX, VD_AY, VD_AZ, VD_N };
+enum { VF_TEMP, VF_PDT, VF_PSX, VF_PSY, VF_PSZ, VF_N };
+enum { LD_P2X, LD_P2Y, LD_P2Z, LD_A1X, LD_A1Y, LD_A1Z, LD_A2X, LD_A2Y, LD_A2Z, LD_FNX, LD_FNY, LD_FNZ,
+       LD_FPX, LD_FPY, LD_FPZ, LD_MNX, LD_MNY, LD_MNZ, LD_MPX, LD_MPY, LD_MPZ, LD_REST, LD_N };
+enum { LF_STRAIN, LF_MAXS, LF_SOFF, LF_STRESS, LF_RATIO, LF_TAREA, LF_TSS, LF_N };
+
+struct VxImpl {
+  // mirror
+  std::vector<double> vd[VD_N];
+  std::vector<float> vf[VF_N];
+  std::vector<uint32_t> vflags;
+  std::vector<double> ld[LD_N];
+  std::vector<float> lf[LF_N];
+  std::vector<uint32_t> lflags;  // small angle, local velocity valid, axis << 8
+  float time = 0.0f;
+
+  // lattice lookups
+  std::unordered_map<uint64_t, CVX_Voxel*> vmap;
+  std::unordered_map<uint64_t, CVX_Link*> lmap[3];
+
+  // engine and synchronisation state
+  vxg_engine* eng = nullptr;
+  int device = 0;
+  int precision = VXG_FP64;
+  bool topo_dirty = true;    // counts or connectivity changed: full re-upload
+  bool tables_dirty = true;  // materials / externals changed
+  bool state_dirty = true;   // host mirror edited
+  bool device_ahead = false; // device state newer than the mirror
+  bool nearby_dirty = true;  // collision lattice lists need regeneration
+  std::map<float, int> powf_slots;  // exponent -> table slot already on the device
+  std::string err;
+
+  static uint64_t key(int x, int y, int z) {
+    const uint64_t B = 1u << 20;
+    return ((uint64_t)(x + B) << 42) | ((uint64_t)(y + B) << 21) | (uint64_t)(z + B);
+  }
+  void push_voxel() {
+    for (auto& a : vd) a.push_back(0.0);
+    for (auto& a : vf) a.push_back(0.0f);
+    vflags.push_back(0);
+  }
+  void push_link() {
+    for (auto& a : ld) a.push_back(0.0);
+    for (auto& a : lf) a.push_back(0.0f);
+    lflags.push_back(0);
+  }
+  void erase_voxel(int i) {
+    for (auto& a : vd) a.erase(a.begin() + i);
+    for (auto& a : vf) a.erase(a.begin() + i);
+    vflags.erase(vflags.begin() + i);
+  }
+  void erase_link(int i) {
+    for (auto& a : ld) a.erase(a.begin() + i);
+    for (auto& a : lf) a.erase(a.begin() + i);
+    lflags.erase(lflags.begin() + i);
+  }
+  void clear_mirror() {
+    for (auto& a : vd) a.clear();
+    for (auto& a : vf) a.clear();
+    vflags.clear();
+    for (auto& a : ld) a.clear();
+    for (auto& a : lf) a.clear();
+    lflags.clear();
+    vmap.clear();
+    for (auto& m : lmap) m.clear();
+  }
+};

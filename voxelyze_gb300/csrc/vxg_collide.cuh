@@ -1,0 +1,491 @@
+// Collision stage of the time step: CVoxelyze::updateCollisions / regenerateCollisions and
+// CVX_Collision::updateContactForce (src/Voxelyze.cpp:670-750, src/VX_Collision.cpp:15-56).
+//
+// Per step, on the engine stream:
+//   c_check    each surface voxel tests its drift from the position at the last rebuild (float
+//              copy, double distance, as the reference) and raises the device "stale" flag
+//   rebuild    only when stale (each kernel exits at once otherwise):
+//              c_insert  surface voxels into a uniform hash grid (cell = watch radius), open
+//                        addressing on the packed cell key, one linked list per cell
+//              c_count   each surface voxel counts partners within the watch radius that are not
+//                        lattice neighbours (the 5-hop list, binary search) - all, and those after it
+//              c_scan    exclusive scans give each voxel its slot in the pair list and in the
+//                        contact list
+//              c_fill    each voxel sorts its partners; pairs (i, j > i) land in the reference's
+//                        list order (i ascending, then j ascending)
+//              c_watch   each voxel's contact list: partners ascending, with the pair index found
+//                        in the partner's sorted list (the order the reference's colWatch ends in)
+//   c_contact  one thread per pair: the penalty + damping contact force (float math)
+// The voxel pass subtracts each voxel's contact forces in its contact-list order.
+#pragma once
+
+struct ColCtl {
+  int stale;        // rebuild needed this step
+  int force_stale;  // set by the host when topology or the collision switch changed
+  int npairs;
+  int nwatch;
+  int status;       // overflow bits
+  int rebuilds;
+};
+
+enum { VXG_COL_ST_PAIR_OVERFLOW = 1, VXG_COL_ST_WATCH_OVERFLOW = 2, VXG_COL_ST_LOCAL_OVERFLOW = 4,
+       VXG_COL_ST_HASH_FULL = 8 };
+
+constexpr int kMaxPartners = 128;
+
+struct ColView {
+  int nv;
+  unsigned long long hcap_mask;
+  const double* pos;
+  const double* linMom;
+  const int* vmat;
+  const uint32_t* vflags;
+  const float* temp;
+  const vxg_voxel_material* vm;
+  const int* nbOff;
+  const int* nbItem;
+  float* lastWatch;          // 3 nv
+  unsigned long long* hkey;  // hcap
+  int* hhead;                // hcap
+  int* next;                 // nv
+  int* cntGt;                // nv
+  int* cntAll;               // nv
+  int* pairOff;              // nv + 1
+  int* watchOff;             // nv + 1
+  int* watchPartner;         // wcap
+  int* watchItem;            // wcap
+  int* pairI;                // pcap
+  int* pairJ;
+  float* pairStiff;
+  float* pairDamp;
+  float* pairForce;          // 3 pcap
+  int pcap, wcap;
+  double cell;               // hash cell edge
+  double thr;                // watch radius squared (float value promoted)
+  double recalc2;            // recalc distance squared (float value promoted)
+  ColCtl* cc;
+  vx64::Ctl* ctl;
+};
+
+__device__ __forceinline__ unsigned long long cell_key(long long cx, long long cy, long long cz) {
+  const long long B = 1ll << 20;
+  return ((unsigned long long)((cx + B) & 0x1FFFFF) << 42) | ((unsigned long long)((cy + B) & 0x1FFFFF) << 21) |
+         (unsigned long long)((cz + B) & 0x1FFFFF);
+}
+__device__ __forceinline__ unsigned long long hash64(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+__device__ __forceinline__ bool is_surface(const ColView& C, int v) { return !(C.vflags[v] & VXG_VF_INTERIOR); }
+
+__global__ void c_check(ColView C) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (C.ctl->halt || C.ctl->diverged) return;
+  if (v == 0 && C.cc->force_stale) C.cc->stale = 1;
+  if (v >= C.nv || !is_surface(C, v)) return;
+  double dx = C.pos[v] - C.lastWatch[v], dy = C.pos[C.nv + v] - C.lastWatch[C.nv + v],
+         dz = C.pos[2 * C.nv + v] - C.lastWatch[2 * C.nv + v];
+  if (dx * dx + dy * dy + dz * dz > C.recalc2) C.cc->stale = 1;
+}
+
+__global__ void c_clear(ColView C) {
+  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i <= C.hcap_mask;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    C.hkey[i] = ~0ull;
+    C.hhead[i] = -1;
+  }
+}
+
+__device__ __forceinline__ void cell_of(const ColView& C, int v, long long* c) {
+  c[0] = (long long)floor(C.pos[v] / C.cell);
+  c[1] = (long long)floor(C.pos[C.nv + v] / C.cell);
+  c[2] = (long long)floor(C.pos[2 * C.nv + v] / C.cell);
+}
+
+__global__ void c_insert(ColView C) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
+  if (v >= C.nv || !is_surface(C, v)) return;
+  C.lastWatch[v] = (float)C.pos[v];
+  C.lastWatch[C.nv + v] = (float)C.pos[C.nv + v];
+  C.lastWatch[2 * C.nv + v] = (float)C.pos[2 * C.nv + v];
+  long long c[3];
+  cell_of(C, v, c);
+  unsigned long long k = cell_key(c[0], c[1], c[2]);
+  unsigned long long h = hash64(k) & C.hcap_mask;
+  for (unsigned long long probe = 0; probe <= C.hcap_mask; ++probe) {
+    unsigned long long prev = atomicCAS(&C.hkey[h], ~0ull, k);
+    if (prev == ~0ull || prev == k) {
+      C.next[v] = atomicExch(&C.hhead[h], v);
+      return;
+    }
+    h = (h + 1) & C.hcap_mask;
+  }
+  atomicOr(&C.cc->status, VXG_COL_ST_HASH_FULL);
+}
+
+__device__ __forceinline__ int find_cell(const ColView& C, unsigned long long k) {
+  unsigned long long h = hash64(k) & C.hcap_mask;
+  for (unsigned long long probe = 0; probe <= C.hcap_mask; ++probe) {
+    unsigned long long cur = C.hkey[h];
+    if (cur == k) return C.hhead[h];
+    if (cur == ~0ull) return -1;
+    h = (h + 1) & C.hcap_mask;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ bool in_sorted(const int* a, int n, int x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < n && a[lo] == x;
+}
+
+// is (v, u) a collision pair of regenerateCollisions (Voxelyze.cpp:735-745)?
+__device__ __forceinline__ bool is_pair(const ColView& C, int v, int u) {
+  int i = v < u ? v : u, j = v < u ? u : v;
+  double dx = C.pos[i] - C.pos[j], dy = C.pos[C.nv + i] - C.pos[C.nv + j], dz = C.pos[2 * C.nv + i] - C.pos[2 * C.nv + j];
+  if (dx * dx + dy * dy + dz * dz > C.thr) return false;
+  int b = C.nbOff[i], e = C.nbOff[i + 1];
+  return !in_sorted(C.nbItem + b, e - b, j);
+}
+
+template <class F>
+__device__ __forceinline__ void for_partners(const ColView& C, int v, F&& f) {
+  long long c[3];
+  cell_of(C, v, c);
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        int u = find_cell(C, cell_key(c[0] + dx, c[1] + dy, c[2] + dz));
+        for (; u >= 0; u = C.next[u])
+          if (u != v && is_pair(C, v, u)) f(u);
+      }
+}
+
+__global__ void c_count(ColView C) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
+  if (v >= C.nv) return;
+  int all = 0, gt = 0;
+  if (is_surface(C, v)) for_partners(C, v, [&](int u) { all++; gt += u > v; });
+  C.cntAll[v] = all;
+  C.cntGt[v] = gt;
+}
+
+// exclusive scans of cntGt -> pairOff and cntAll -> watchOff (one block; rebuilds are rare)
+__global__ void c_scan(ColView C) {
+  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
+  __shared__ int sg[1024], sa[1024];
+  int t = threadIdx.x, T = blockDim.x;
+  int chunk = (C.nv + T - 1) / T;
+  int b = t * chunk, e = min(C.nv, b + chunk);
+  int g = 0, a = 0;
+  for (int i = b; i < e; ++i) { g += C.cntGt[i]; a += C.cntAll[i]; }
+  sg[t] = g;
+  sa[t] = a;
+  __syncthreads();
+  for (int o = 1; o < T; o <<= 1) {
+    int vg = t >= o ? sg[t - o] : 0, va = t >= o ? sa[t - o] : 0;
+    __syncthreads();
+    sg[t] += vg;
+    sa[t] += va;
+    __syncthreads();
+  }
+  int pg = sg[t] - g, pa = sa[t] - a;
+  for (int i = b; i < e; ++i) {
+    C.pairOff[i] = pg;
+    C.watchOff[i] = pa;
+    pg += C.cntGt[i];
+    pa += C.cntAll[i];
+  }
+  if (t == T - 1) {
+    C.pairOff[C.nv] = sg[t];
+    C.watchOff[C.nv] = sa[t];
+    C.cc->npairs = sg[t];
+    C.cc->nwatch = sa[t];
+    if (sg[t] > C.pcap) atomicOr(&C.cc->status, VXG_COL_ST_PAIR_OVERFLOW);
+    if (sa[t] > C.wcap) atomicOr(&C.cc->status, VXG_COL_ST_WATCH_OVERFLOW);
+  }
+}
+
+__global__ void c_fill(ColView C) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged || C.cc->status) return;
+  if (v >= C.nv || !is_surface(C, v)) return;
+  int buf[kMaxPartners];
+  int n = 0;
+  for_partners(C, v, [&](int u) {
+    if (n < kMaxPartners) buf[n] = u;
+    n++;
+  });
+  if (n > kMaxPartners) {
+    atomicOr(&C.cc->status, VXG_COL_ST_LOCAL_OVERFLOW);
+    return;
+  }
+  for (int i = 1; i < n; ++i) {  // insertion sort, ascending
+    int x = buf[i], j = i - 1;
+    while (j >= 0 && buf[j] > x) { buf[j + 1] = buf[j]; --j; }
+    buf[j + 1] = x;
+  }
+  int wo = C.watchOff[v], po = C.pairOff[v], r = 0;
+  const vxg_voxel_material& m1 = C.vm[C.vmat[v]];
+  for (int i = 0; i < n; ++i) {
+    int u = buf[i];
+    C.watchPartner[wo + i] = u;
+    if (u > v) {
+      const vxg_voxel_material& m2 = C.vm[C.vmat[u]];
+      int c = po + r++;
+      C.pairI[c] = v;
+      C.pairJ[c] = u;
+      // CVX_Collision::CVX_Collision  VX_Collision.cpp:17-23
+      C.pairStiff[c] = 2.0f / (1.0f / m1.penetrationStiffness + 1.0f / m2.penetrationStiffness);
+      C.pairDamp[c] = 0.5f * (m1.zetaCollision * m1.c2xSqMxExS + m2.zetaCollision * m2.c2xSqMxExS);
+    }
+  }
+}
+
+__global__ void c_watch(ColView C) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged || C.cc->status) return;
+  if (v >= C.nv) return;
+  int wo = C.watchOff[v], n = C.cntAll[v];
+  int nLess = n - C.cntGt[v];
+  for (int k = 0; k < n; ++k) {
+    int u = C.watchPartner[wo + k];
+    int item;
+    if (u > v) {
+      item = (C.pairOff[v] + (k - nLess)) * 2;
+    } else {
+      int uo = C.watchOff[u], ul = C.cntAll[u] - C.cntGt[u];
+      const int* seg = C.watchPartner + uo + ul;
+      int lo = 0, hi = C.cntGt[u];
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (seg[mid] < v) lo = mid + 1;
+        else hi = mid;
+      }
+      item = (C.pairOff[u] + lo) * 2 + 1;
+    }
+    C.watchItem[wo + k] = item;
+  }
+}
+
+// CVX_Voxel::baseSizeAverage for the envelope  VX_Voxel.h:90
+__device__ __forceinline__ double col_bsa(const ColView& C, int v) {
+  const vxg_voxel_material& m = C.vm[C.vmat[v]];
+  float f = 1 + C.temp[v] * m.alphaCTE;
+  return ((double)f * m.size[0] + (double)f * m.size[1] + (double)f * m.size[2]) / 3.0f;
+}
+
+// CVX_Collision::updateContactForce  VX_Collision.cpp:42-56
+__global__ void c_contact(ColView C) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (C.ctl->halt || C.ctl->diverged) return;
+  if (c == 0) {
+    if (C.cc->stale) C.cc->rebuilds += 1;
+    C.cc->stale = 0;
+    C.cc->force_stale = 0;
+    if (C.cc->status) atomicOr(&C.ctl->status, C.cc->status << 8);
+  }
+  if (c >= C.cc->npairs || C.cc->status) return;
+  int a = C.pairI[c], b = C.pairJ[c];
+  int nv = C.nv;
+  float ox = (float)(C.pos[b] - C.pos[a]), oy = (float)(C.pos[nv + b] - C.pos[nv + a]),
+        oz = (float)(C.pos[2 * nv + b] - C.pos[2 * nv + a]);
+  float nom = (float)((col_bsa(C, a) + col_bsa(C, b)) * 0.625f);
+  float rel = nom - sqrtf(ox * ox + oy * oy + oz * oz);
+  float fx = 0, fy = 0, fz = 0;
+  if (rel > 0) {
+    float l = sqrtf(ox * ox + oy * oy + oz * oz);
+    float ux = ox, uy = oy, uz = oz;
+    if (l > 0) {
+      float inv = (float)1.0 / l;
+      ux = inv * ox; uy = inv * oy; uz = inv * oz;
+    }
+    const vxg_voxel_material& m1 = C.vm[C.vmat[a]];
+    const vxg_voxel_material& m2 = C.vm[C.vmat[b]];
+    double v1x = m1.massInv * C.linMom[a], v1y = m1.massInv * C.linMom[nv + a], v1z = m1.massInv * C.linMom[2 * nv + a];
+    double v2x = m2.massInv * C.linMom[b], v2y = m2.massInv * C.linMom[nv + b], v2z = m2.massInv * C.linMom[2 * nv + b];
+    float relVel = (float)((v1x * (double)ux + v1y * (double)uy + v1z * (double)uz) -
+                           (v2x * (double)ux + v2y * (double)uy + v2z * (double)uz));
+    float k = C.pairStiff[c] * rel + C.pairDamp[c] * relVel;
+    fx = ux * k; fy = uy * k; fz = uz * k;
+  }
+  C.pairForce[3 * c] = fx;
+  C.pairForce[3 * c + 1] = fy;
+  C.pairForce[3 * c + 2] = fz;
+}
+
+struct Collide {
+  ColView C{};
+  ColCtl* cc = nullptr;
+  char* buf = nullptr;
+  int* d_nb = nullptr;  // nearby CSR storage (offsets then items)
+  int nv = 0;
+  int pcap = 0, wcap = 0;
+  int grid_pairs = 1;
+
+  void release() {
+    if (buf) cudaFree(buf);
+    if (d_nb) cudaFree(d_nb);
+    if (cc) cudaFree(cc);
+    buf = nullptr;
+    d_nb = nullptr;
+    cc = nullptr;
+  }
+  // scene size changed: buffers are (re)allocated when collisions are first used (set_nearby)
+  int resize(int n) {
+    if (buf) cudaFree(buf);
+    buf = nullptr;
+    if (d_nb) cudaFree(d_nb);
+    d_nb = nullptr;
+    C.nbOff = C.nbItem = nullptr;
+    C.watchOff = C.watchItem = nullptr;
+    C.pairForce = nullptr;
+    nv = n;
+    if (!cc) {
+      if (cudaMalloc(&cc, sizeof(ColCtl)) != cudaSuccess) return VXG_E_CUDA;
+    }
+    if (cudaMemset(cc, 0, sizeof(ColCtl)) != cudaSuccess) return VXG_E_CUDA;
+    return VXG_OK;
+  }
+  int allocate() {
+    int n = nv;
+    unsigned long long hcap = 1024;
+    while (hcap < 2ull * (unsigned long long)n) hcap <<= 1;
+    pcap = std::max(1024, 32 * n);
+    wcap = 2 * pcap;
+    size_t bytes = 0;
+    auto take = [&](size_t b) { size_t o = bytes; bytes += (b + 255) / 256 * 256; return o; };
+    size_t o_last = take(sizeof(float) * 3 * (size_t)n);
+    size_t o_hkey = take(8 * hcap), o_hhead = take(4 * hcap);
+    size_t o_next = take(4 * (size_t)n), o_cg = take(4 * (size_t)n), o_ca = take(4 * (size_t)n);
+    size_t o_po = take(4 * ((size_t)n + 1)), o_wo = take(4 * ((size_t)n + 1));
+    size_t o_wp = take(4 * (size_t)wcap), o_wi = take(4 * (size_t)wcap);
+    size_t o_pi = take(4 * (size_t)pcap), o_pj = take(4 * (size_t)pcap), o_ps = take(4 * (size_t)pcap),
+           o_pd = take(4 * (size_t)pcap), o_pf = take(12 * (size_t)pcap);
+    if (n == 0) return VXG_OK;
+    if (cudaMalloc(&buf, bytes) != cudaSuccess) return VXG_E_CUDA;
+    if (cudaMemset(buf, 0, bytes) != cudaSuccess) return VXG_E_CUDA;
+    C.nv = n;
+    C.hcap_mask = hcap - 1;
+    C.lastWatch = (float*)(buf + o_last);
+    C.hkey = (unsigned long long*)(buf + o_hkey);
+    C.hhead = (int*)(buf + o_hhead);
+    C.next = (int*)(buf + o_next);
+    C.cntGt = (int*)(buf + o_cg);
+    C.cntAll = (int*)(buf + o_ca);
+    C.pairOff = (int*)(buf + o_po);
+    C.watchOff = (int*)(buf + o_wo);
+    C.watchPartner = (int*)(buf + o_wp);
+    C.watchItem = (int*)(buf + o_wi);
+    C.pairI = (int*)(buf + o_pi);
+    C.pairJ = (int*)(buf + o_pj);
+    C.pairStiff = (float*)(buf + o_ps);
+    C.pairDamp = (float*)(buf + o_pd);
+    C.pairForce = (float*)(buf + o_pf);
+    C.pcap = pcap;
+    C.wcap = wcap;
+    C.cc = cc;
+    grid_pairs = std::max(1, (pcap + 255) / 256);
+    return VXG_OK;
+  }
+  int set_nearby(int n, const int* off, const int* items, long long n_items, cudaStream_t s) {
+    if (n != nv) return VXG_E_SIZE;
+    if (!buf) {
+      int rc = allocate();
+      if (rc) return rc;
+    }
+    if (d_nb) cudaFree(d_nb);
+    d_nb = nullptr;
+    size_t tot = (size_t)(n + 1) + (size_t)std::max<long long>(n_items, 1);
+    if (cudaMalloc(&d_nb, 4 * tot) != cudaSuccess) return VXG_E_CUDA;
+    if (cudaMemcpyAsync(d_nb, off, 4 * (size_t)(n + 1), cudaMemcpyHostToDevice, s) != cudaSuccess) return VXG_E_CUDA;
+    if (n_items > 0 &&
+        cudaMemcpyAsync(d_nb + n + 1, items, 4 * (size_t)n_items, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return VXG_E_CUDA;
+    int one = 1;
+    if (cudaMemcpyAsync(&cc->force_stale, &one, 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return VXG_E_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return VXG_E_CUDA;
+    C.nbOff = d_nb;
+    C.nbItem = d_nb + n + 1;
+    return VXG_OK;
+  }
+  void bind(View& S) {
+    C.pos = S.pos;
+    C.linMom = S.linMom;
+    C.vmat = S.vmat;
+    C.vflags = S.vflags;
+    C.temp = S.temp;
+    C.vm = S.vm;
+    C.ctl = S.ctl;
+    S.colOff = C.watchOff;
+    S.colItem = C.watchItem;
+    S.colForce = C.pairForce;
+  }
+  void enqueue(const vxg_globals& g, cudaStream_t s) {
+    if (!buf || !C.nbOff) return;
+    float watchVx = 2 * g.boundingRadius + g.watchDistance;
+    float watchMm = (float)(g.voxSize * watchVx);
+    float recalc = (float)(g.voxSize * g.watchDistance / 2);
+    C.thr = (double)(watchMm * watchMm);
+    C.recalc2 = (double)(recalc * recalc);
+    C.cell = (double)watchMm * 1.001;
+    int gv = std::max(1, (nv + 255) / 256);
+    c_check<<<gv, 256, 0, s>>>(C);
+    c_clear<<<256, 256, 0, s>>>(C);
+    c_insert<<<gv, 256, 0, s>>>(C);
+    c_count<<<gv, 256, 0, s>>>(C);
+    c_scan<<<1, 1024, 0, s>>>(C);
+    c_fill<<<gv, 128, 0, s>>>(C);
+    c_watch<<<gv, 256, 0, s>>>(C);
+    c_contact<<<grid_pairs, 256, 0, s>>>(C);
+  }
+  int get_pairs(int* out, int cap, int* n, cudaStream_t s) {
+    *n = 0;
+    if (!cc) return VXG_OK;
+    ColCtl h;
+    if (cudaMemcpyAsync(&h, cc, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess) return VXG_E_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return VXG_E_CUDA;
+    *n = h.npairs;
+    int m = std::min(cap, h.npairs);
+    if (m > 0 && out) {
+      std::vector<int> a(m), b(m);
+      if (cudaMemcpyAsync(a.data(), C.pairI, 4 * (size_t)m, cudaMemcpyDeviceToHost, s) != cudaSuccess) return VXG_E_CUDA;
+      if (cudaMemcpyAsync(b.data(), C.pairJ, 4 * (size_t)m, cudaMemcpyDeviceToHost, s) != cudaSuccess) return VXG_E_CUDA;
+      if (cudaStreamSynchronize(s) != cudaSuccess) return VXG_E_CUDA;
+      for (int k = 0; k < m; ++k) { out[2 * k] = a[k]; out[2 * k + 1] = b[k]; }
+    }
+    return VXG_OK;
+  }
+  int rebuilds() {
+    if (!cc) return 0;
+    ColCtl h;
+    cudaMemcpy(&h, cc, sizeof(h), cudaMemcpyDeviceToHost);
+    return h.rebuilds;
+  }
+  int pairs(cudaStream_t) {
+    if (!cc) return 0;
+    ColCtl h;
+    cudaMemcpy(&h, cc, sizeof(h), cudaMemcpyDeviceToHost);
+    return h.npairs;
+  }
+  const char* status_message(int st) {
+    int c = st >> 8;
+    if (c & VXG_COL_ST_PAIR_OVERFLOW) return "collision pair list overflow";
+    if (c & VXG_COL_ST_WATCH_OVERFLOW) return "collision contact list overflow";
+    if (c & VXG_COL_ST_LOCAL_OVERFLOW) return "more than 128 collision partners for one voxel";
+    if (c & VXG_COL_ST_HASH_FULL) return "collision hash table full";
+    return "device status error";
+  }
+};

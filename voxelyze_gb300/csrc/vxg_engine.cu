@@ -1,0 +1,705 @@
+// GB300 time-step engine: device state, sm_103a kernels and the vxg_* C ABI (include/vxg.h).
+//
+// One step of CVoxelyze::doTimeStep (src/Voxelyze.cpp:251-284) is, on one CUDA stream:
+//   k_poisson   Poisson-strain cache pre-pass (only when some material has nu != 0); fills the
+//               cache the reference fills lazily from the previous step's link strains
+//               (src/VX_Voxel.cpp:336-343, first touched in the link pass at src/VX_Link.cpp:160)
+//   k_link      one thread per link: CVX_Link::updateForces; with dt < 0 it first evaluates
+//               recommendedTimeStep's per-link term (with its side effects) and reduces the maximum
+//               with warp shuffles and one atomic per block; flags divergence (strain > 100)
+//   collisions  when enabled (vxg_collide.cuh)
+//   k_voxel     one thread per voxel: CVX_Voxel::timeStep; gathers its 6 link slots in direction
+//               order, no atomics; skips the step when the link pass diverged
+// Batches of steps are enqueued back to back and, for repeated batch shapes, replayed from a
+// captured CUDA graph.  Nothing is synchronised inside a batch; the host reads the control block
+// once per batch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "vx_phys64.cuh"
+#include "vxg.h"
+
+using vx64::Ctl;
+using vx64::View;
+
+namespace {
+
+constexpr int kBlock = 256;
+
+// ---------------------------------------------------------------------------------------------
+// kernels
+__global__ void k_poisson(View S) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= S.nv) return;
+  if (S.ctl->halt) return;
+  uint32_t f = S.vflags[v];
+  if (!(f & VXG_VF_PSTRAIN_INVALID)) return;
+  if (S.vm[S.vmat[v]].nu == 0) return;
+  bool any = false;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) any |= S.vlinks[i * S.nv + v] >= 0;
+  if (!any) return;
+  float p[3];
+  vx64::poisson_strain(S, v, p);
+  S.pStrain[v] = p[0];
+  S.pStrain[S.nv + v] = p[1];
+  S.pStrain[2 * S.nv + v] = p[2];
+  S.vflags[v] = f & ~(uint32_t)VXG_VF_PSTRAIN_INVALID;
+}
+
+__device__ __forceinline__ void block_max_to(unsigned* dst, float f) {
+  // warp max then one atomic per warp; NaN never wins (the reference's `>` test), negatives lose to 0
+  unsigned u = (f > 0.0f) ? __float_as_uint(f) : 0u;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) u = max(u, __shfl_xor_sync(0xffffffffu, u, o));
+  if ((threadIdx.x & 31) == 0 && u) atomicMax(dst, u);
+}
+
+template <bool RECOMMEND, bool FORCES>
+__global__ void __launch_bounds__(kBlock) k_link(View S, int parity) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (S.ctl->halt) return;
+  float f2 = 0.0f;
+  bool live = l < S.nl;
+  if (RECOMMEND && live) {
+    uint32_t lf = S.lflags[l];
+    int vn = S.lvox[l], vp = S.lvox[S.nl + l];
+    f2 = vx64::link_freq2(S, l, vn, vp, (lf >> 8) & 3, S.lm[S.lmat[l]]);
+  }
+  if (RECOMMEND) block_max_to(&S.ctl->maxf[parity], f2);
+  if (!FORCES || !live) return;
+  vx64::link_update(S, l);
+  if (S.strain[l] > 100) S.ctl->diverged = 1;
+}
+
+// dt of this step: fixed, or 1/(2 pi sqrt(max)) from the link pass (Voxelyze.cpp:302-310)
+__device__ __forceinline__ float step_dt(const View& S, bool recommend, float dt_fixed, int parity,
+                                         float fallback) {
+  if (!recommend) return dt_fixed;
+  float mx = __uint_as_float(S.ctl->maxf[parity]);
+  if (mx <= 0.0f) mx = fallback;
+  if (mx <= 0.0f) return 0.0f;
+  return 1.0f / (6.283185f * sqrtf(mx));
+}
+
+template <bool RECOMMEND>
+__global__ void __launch_bounds__(kBlock) k_voxel(View S, float dt_fixed, int parity, float fallback) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (S.ctl->halt) return;
+  if (S.ctl->diverged) {
+    if (v == 0) S.ctl->halt = 1;
+    return;
+  }
+  float dt = step_dt(S, RECOMMEND, dt_fixed, parity, fallback);
+  if (v == 0) {
+    S.ctl->steps += 1;
+    S.ctl->time += dt;
+    S.ctl->last_dt = dt;
+    if (RECOMMEND) S.ctl->maxf[parity ^ 1] = 0u;  // next step's slot; nobody reads it in this pass
+  }
+  if (v >= S.nv) return;
+  vx64::voxel_update(S, v, dt);
+}
+
+// setAmbientTemperature(t, true): every voxel's temperature, then every link's rest length
+// (src/Voxelyze.cpp:585-594, src/VX_Voxel.cpp:108-114, src/VX_Link.cpp:137-140)
+__global__ void k_set_temp(View S, float t) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < S.nv) S.temp[v] = t;
+}
+__global__ void k_rest_length(View S) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= S.nl) return;
+  int axis = (S.lflags[l] >> 8) & 3;
+  S.rest[l] = 0.5 * (vx64::base_size(S, S.lvox[l], axis) + vx64::base_size(S, S.lvox[S.nl + l], axis));
+}
+
+// stateInfo reductions (Voxelyze.cpp:752-800): per element value, block partials in double
+__device__ float info_value(const View& S, int info, int i) {
+  if (info == 5) return S.stress[i];
+  if (info == 6) return S.strain[i];
+  if (info == 7) {
+    const vxg_link_material& m = S.lm[S.lmat[i]];
+    int nl = S.nl;
+    double fnx = S.fN[i], mnx = S.mN[i], mny = S.mN[nl + i], mnz = S.mN[2 * nl + i];
+    double mpy = S.mP[nl + i], mpz = S.mP[2 * nl + i];
+    return (float)(fnx * fnx / (2.0f * m.a1) + mnx * mnx / (2.0 * m.a2) + (mnz * mnz - mnz * mpz + mpz * mpz) / (3.0 * m.b3) +
+                   (mny * mny - mny * mpy + mpy * mpy) / (3.0 * m.b3));
+  }
+  const vxg_voxel_material& m = S.vm[S.vmat[i]];
+  int nv = S.nv;
+  double s = m.nomSize;
+  switch (info) {
+    case 0: {
+      double dx = S.pos[i] - S.vidx[i] * s, dy = S.pos[nv + i] - S.vidx[nv + i] * s, dz = S.pos[2 * nv + i] - S.vidx[2 * nv + i] * s;
+      return (float)sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    case 1: {
+      double x = S.linMom[i], y = S.linMom[nv + i], z = S.linMom[2 * nv + i];
+      return (float)(sqrt(x * x + y * y + z * z) * m.massInv);
+    }
+    case 2: {
+      double x = S.linMom[i], y = S.linMom[nv + i], z = S.linMom[2 * nv + i];
+      double a = S.angMom[i], b = S.angMom[nv + i], c = S.angMom[2 * nv + i];
+      return (float)(0.5 * (m.massInv * (x * x + y * y + z * z) + m.inertiaInv * (a * a + b * b + c * c)));
+    }
+    case 3: {
+      double w = S.orient[i];
+      int f = 0;
+      return (float)(2.0 * vxm::cr_acos(w > 1 ? 1 : w, &f));
+    }
+    case 4: {
+      double a = S.angMom[i], b = S.angMom[nv + i], c = S.angMom[2 * nv + i];
+      return (float)(sqrt(a * a + b * b + c * c) * m.inertiaInv);
+    }
+    case 9: return m.mass;
+    default: return 0.0f;
+  }
+}
+__global__ void k_reduce(View S, int info, int n, double* out /* 3 per block: min, max, sum */) {
+  __shared__ double smin[kBlock / 32], smax[kBlock / 32], ssum[kBlock / 32];
+  double mn = 3.4e38, mx = -3.4e38, sm = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float t = info_value(S, info, i);
+    mn = t < mn ? t : mn;
+    mx = t > mx ? t : mx;
+    sm += t;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    sm += __shfl_xor_sync(0xffffffffu, sm, o);
+  }
+  int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { smin[w] = mn; smax[w] = mx; ssum[w] = sm; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < kBlock / 32; ++k) { mn = fmin(mn, smin[k]); mx = fmax(mx, smax[k]); sm += ssum[k]; }
+    out[3 * blockIdx.x] = mn;
+    out[3 * blockIdx.x + 1] = mx;
+    out[3 * blockIdx.x + 2] = sm;
+  }
+}
+
+int grid_for(int n) { return std::max(1, (n + kBlock - 1) / kBlock); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+struct FieldDesc {
+  size_t elem;  // bytes per element
+  int comps;    // elements per voxel or link
+  bool per_link;
+};
+
+static FieldDesc field_desc(int f) {
+  switch (f) {
+    case VXG_F_VOXEL_MATERIAL: return {4, 1, false};
+    case VXG_F_VOXEL_INDEX: return {4, 3, false};
+    case VXG_F_VOXEL_LINKS: return {4, 6, false};
+    case VXG_F_VOXEL_EXTERNAL: return {4, 1, false};
+    case VXG_F_POS: return {8, 3, false};
+    case VXG_F_LINMOM: return {8, 3, false};
+    case VXG_F_ORIENT: return {8, 4, false};
+    case VXG_F_ANGMOM: return {8, 3, false};
+    case VXG_F_TEMP: return {4, 1, false};
+    case VXG_F_PREV_DT: return {4, 1, false};
+    case VXG_F_PSTRAIN: return {4, 3, false};
+    case VXG_F_VOXEL_FLAGS: return {4, 1, false};
+    case VXG_F_LINK_VOXELS: return {4, 2, true};
+    case VXG_F_LINK_MATERIAL: return {4, 1, true};
+    case VXG_F_LINK_FLAGS: return {4, 1, true};
+    case VXG_F_POS2: case VXG_F_ANGLE1V: case VXG_F_ANGLE2V: case VXG_F_FORCE_NEG: case VXG_F_FORCE_POS:
+    case VXG_F_MOMENT_NEG: case VXG_F_MOMENT_POS: return {8, 3, true};
+    case VXG_F_REST_LENGTH: return {8, 1, true};
+    case VXG_F_STRAIN: case VXG_F_MAX_STRAIN: case VXG_F_STRAIN_OFFSET: case VXG_F_STRESS:
+    case VXG_F_STRAIN_RATIO: case VXG_F_TRANSVERSE_AREA: case VXG_F_TRANSVERSE_STRAIN_SUM: return {4, 1, true};
+    default: return {0, 0, false};
+  }
+}
+
+#include "vxg_collide.cuh"
+
+struct vxg_engine {
+  int device = 0;
+  int precision = VXG_FP64;
+  int nv = 0, nl = 0;
+  cudaStream_t stream = nullptr;
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  void* field_ptr[VXG_F_COUNT] = {};
+  View S{};
+  Ctl* ctl = nullptr;
+  vxg_voxel_material* d_vm = nullptr;
+  vxg_link_material* d_lm = nullptr;
+  vxg_external* d_ext = nullptr;
+  int n_vm = 0, n_lm = 0, n_ext = 0;
+  float* d_powtab = nullptr;
+  int n_powslots = 0;
+  double* d_partials = nullptr;
+  vxg_globals g{};
+  bool have_globals = false;
+  Collide col;
+  bool timing = false;
+  cudaEvent_t ev[4] = {};
+  std::vector<cudaEvent_t> tev;  // timing mode: 4 events per step of the last batch
+  int tev_used = 0;
+  float t_link = 0, t_col = 0, t_vox = 0, t_batch = 0;
+  std::string err;
+  // captured batches
+  cudaGraphExec_t graph = nullptr;
+  int graph_n = -1;
+  float graph_dt = 0;
+  bool graph_valid = false;
+};
+
+static int fail(vxg_engine* e, int code, const char* what, cudaError_t ce = cudaSuccess) {
+  if (e) {
+    e->err = what;
+    if (ce != cudaSuccess) {
+      e->err += ": ";
+      e->err += cudaGetErrorString(ce);
+    }
+  }
+  return code;
+}
+#define VXG_CK(call)                                                     \
+  do {                                                                   \
+    cudaError_t _c = (call);                                             \
+    if (_c != cudaSuccess) return fail(e, VXG_E_CUDA, #call, _c);        \
+  } while (0)
+
+static void release_arena(vxg_engine* e) {
+  if (e->arena) cudaFree(e->arena);
+  e->arena = nullptr;
+  e->arena_bytes = 0;
+  std::memset(e->field_ptr, 0, sizeof(e->field_ptr));
+}
+
+static void rebuild_view(vxg_engine* e) {
+  View& S = e->S;
+  S.nv = e->nv;
+  S.nl = e->nl;
+  auto P = [&](int f) { return e->field_ptr[f]; };
+  S.vmat = (const int*)P(VXG_F_VOXEL_MATERIAL);
+  S.vidx = (const int*)P(VXG_F_VOXEL_INDEX);
+  S.vlinks = (const int*)P(VXG_F_VOXEL_LINKS);
+  S.vext = (const int*)P(VXG_F_VOXEL_EXTERNAL);
+  S.vflags = (uint32_t*)P(VXG_F_VOXEL_FLAGS);
+  S.pos = (double*)P(VXG_F_POS);
+  S.linMom = (double*)P(VXG_F_LINMOM);
+  S.orient = (double*)P(VXG_F_ORIENT);
+  S.angMom = (double*)P(VXG_F_ANGMOM);
+  S.temp = (float*)P(VXG_F_TEMP);
+  S.prevDt = (float*)P(VXG_F_PREV_DT);
+  S.pStrain = (float*)P(VXG_F_PSTRAIN);
+  S.lvox = (const int*)P(VXG_F_LINK_VOXELS);
+  S.lmat = (const int*)P(VXG_F_LINK_MATERIAL);
+  S.lflags = (uint32_t*)P(VXG_F_LINK_FLAGS);
+  S.pos2 = (double*)P(VXG_F_POS2);
+  S.a1v = (double*)P(VXG_F_ANGLE1V);
+  S.a2v = (double*)P(VXG_F_ANGLE2V);
+  S.fN = (double*)P(VXG_F_FORCE_NEG);
+  S.fP = (double*)P(VXG_F_FORCE_POS);
+  S.mN = (double*)P(VXG_F_MOMENT_NEG);
+  S.mP = (double*)P(VXG_F_MOMENT_POS);
+  S.rest = (double*)P(VXG_F_REST_LENGTH);
+  S.strain = (float*)P(VXG_F_STRAIN);
+  S.maxStrain = (float*)P(VXG_F_MAX_STRAIN);
+  S.strainOffset = (float*)P(VXG_F_STRAIN_OFFSET);
+  S.stress = (float*)P(VXG_F_STRESS);
+  S.strainRatio = (float*)P(VXG_F_STRAIN_RATIO);
+  S.tArea = (float*)P(VXG_F_TRANSVERSE_AREA);
+  S.tSS = (float*)P(VXG_F_TRANSVERSE_STRAIN_SUM);
+  S.vm = e->d_vm;
+  S.lm = e->d_lm;
+  S.ext = e->d_ext;
+  S.powtab = e->d_powtab;
+  S.ctl = e->ctl;
+  e->col.bind(S);
+  e->graph_valid = false;
+}
+
+template <class T>
+static int upload_table(vxg_engine* e, T** dptr, int* have, const T* src, int n) {
+  if (n > *have || !*dptr) {
+    if (*dptr) cudaFree(*dptr);
+    *dptr = nullptr;
+    cudaError_t c = cudaMalloc(dptr, sizeof(T) * (size_t)std::max(n, 1));
+    if (c != cudaSuccess) return fail(e, VXG_E_CUDA, "table alloc", c);
+    *have = n;
+  }
+  if (n) {
+    cudaError_t c = cudaMemcpyAsync(*dptr, src, sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, e->stream);
+    if (c != cudaSuccess) return fail(e, VXG_E_CUDA, "table copy", c);
+  }
+  return VXG_OK;
+}
+
+extern "C" {
+
+int vxg_create(vxg_engine** out, int device, int precision) {
+  if (!out) return VXG_E_ARG;
+  *out = nullptr;
+  if (precision != VXG_FP64) return VXG_E_ARG;
+  vxg_engine* e = new vxg_engine();
+  e->device = device;
+  e->precision = precision;
+  cudaError_t c = cudaSetDevice(device);
+  if (c != cudaSuccess) { delete e; return VXG_E_CUDA; }
+  c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (c == cudaSuccess) c = cudaMalloc(&e->ctl, sizeof(Ctl));
+  if (c == cudaSuccess) c = cudaMemset(e->ctl, 0, sizeof(Ctl));
+  if (c == cudaSuccess) c = cudaMalloc(&e->d_partials, sizeof(double) * 3 * 4096);
+  for (int i = 0; i < 4 && c == cudaSuccess; ++i) c = cudaEventCreate(&e->ev[i]);
+  if (c != cudaSuccess) { vxg_destroy(e); return VXG_E_CUDA; }
+  *out = e;
+  return VXG_OK;
+}
+
+int vxg_destroy(vxg_engine* e) {
+  if (!e) return VXG_OK;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  release_arena(e);
+  e->col.release();
+  if (e->ctl) cudaFree(e->ctl);
+  if (e->d_vm) cudaFree(e->d_vm);
+  if (e->d_lm) cudaFree(e->d_lm);
+  if (e->d_ext) cudaFree(e->d_ext);
+  if (e->d_powtab) cudaFree(e->d_powtab);
+  if (e->d_partials) cudaFree(e->d_partials);
+  for (int i = 0; i < 4; ++i)
+    if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+  for (cudaEvent_t x : e->tev) cudaEventDestroy(x);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return VXG_OK;
+}
+
+int vxg_precision(const vxg_engine* e) { return e ? e->precision : VXG_E_ARG; }
+
+int vxg_resize(vxg_engine* e, int nv, int nl) {
+  if (!e || nv < 0 || nl < 0) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  release_arena(e);
+  e->nv = nv;
+  e->nl = nl;
+  size_t off[VXG_F_COUNT] = {};
+  size_t total = 0;
+  for (int f = 0; f < VXG_F_TIME; ++f) {
+    FieldDesc d = field_desc(f);
+    size_t n = (size_t)d.comps * (d.per_link ? nl : nv);
+    off[f] = total;
+    total += ((n * d.elem + 255) / 256) * 256;
+  }
+  if (total == 0) total = 256;
+  VXG_CK(cudaMalloc(&e->arena, total));
+  VXG_CK(cudaMemsetAsync(e->arena, 0, total, e->stream));
+  e->arena_bytes = total;
+  for (int f = 0; f < VXG_F_TIME; ++f) e->field_ptr[f] = e->arena + off[f];
+  int rc = e->col.resize(nv);
+  if (rc) return fail(e, rc, "collision buffers");
+  VXG_CK(cudaMemsetAsync(e->ctl, 0, sizeof(Ctl), e->stream));
+  rebuild_view(e);
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  return VXG_OK;
+}
+
+int vxg_set_field(vxg_engine* e, int f, const void* host, long long count) {
+  if (!e || !host || f < 0 || f >= VXG_F_COUNT) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  if (f == VXG_F_TIME) {
+    if (count != 1) return VXG_E_SIZE;
+    VXG_CK(cudaMemcpyAsync(&e->ctl->time, host, 4, cudaMemcpyHostToDevice, e->stream));
+    VXG_CK(cudaStreamSynchronize(e->stream));
+    return VXG_OK;
+  }
+  FieldDesc d = field_desc(f);
+  long long n = (long long)d.comps * (d.per_link ? e->nl : e->nv);
+  if (count != n) return fail(e, VXG_E_SIZE, "vxg_set_field: element count mismatch");
+  if (n == 0) return VXG_OK;
+  VXG_CK(cudaMemcpyAsync(e->field_ptr[f], host, (size_t)n * d.elem, cudaMemcpyHostToDevice, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  return VXG_OK;
+}
+
+int vxg_get_field(vxg_engine* e, int f, void* host, long long count) {
+  if (!e || !host || f < 0 || f >= VXG_F_COUNT) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  if (f == VXG_F_TIME) {
+    if (count != 1) return VXG_E_SIZE;
+    VXG_CK(cudaMemcpyAsync(host, &e->ctl->time, 4, cudaMemcpyDeviceToHost, e->stream));
+    VXG_CK(cudaStreamSynchronize(e->stream));
+    return VXG_OK;
+  }
+  FieldDesc d = field_desc(f);
+  long long n = (long long)d.comps * (d.per_link ? e->nl : e->nv);
+  if (count != n) return fail(e, VXG_E_SIZE, "vxg_get_field: element count mismatch");
+  if (n == 0) return VXG_OK;
+  VXG_CK(cudaMemcpyAsync(host, e->field_ptr[f], (size_t)n * d.elem, cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  return VXG_OK;
+}
+
+int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const vxg_link_material* lm, int n_lm,
+                   const vxg_external* ext, int n_ext) {
+  if (!e || n_vm < 0 || n_lm < 0 || n_ext < 0) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  int rc;
+  if ((rc = upload_table(e, &e->d_vm, &e->n_vm, vm, n_vm))) return rc;
+  if ((rc = upload_table(e, &e->d_lm, &e->n_lm, lm, n_lm))) return rc;
+  if ((rc = upload_table(e, &e->d_ext, &e->n_ext, ext, n_ext))) return rc;
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  rebuild_view(e);
+  return VXG_OK;
+}
+
+int vxg_set_powf_table(vxg_engine* e, int slot, float /*exponent*/, const float* table) {
+  if (!e || slot < 0 || slot > 63 || !table) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  const size_t per = (size_t)1 << 24;
+  if (slot >= e->n_powslots) {
+    float* np = nullptr;
+    int ns = slot + 1;
+    VXG_CK(cudaMalloc(&np, per * sizeof(float) * ns));
+    if (e->d_powtab) {
+      VXG_CK(cudaMemcpyAsync(np, e->d_powtab, per * sizeof(float) * e->n_powslots, cudaMemcpyDeviceToDevice, e->stream));
+      VXG_CK(cudaStreamSynchronize(e->stream));
+      cudaFree(e->d_powtab);
+    }
+    e->d_powtab = np;
+    e->n_powslots = ns;
+  }
+  VXG_CK(cudaMemcpyAsync(e->d_powtab + per * slot, table, per * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  rebuild_view(e);
+  return VXG_OK;
+}
+
+int vxg_set_globals(vxg_engine* e, const vxg_globals* g) {
+  if (!e || !g) return VXG_E_ARG;
+  e->g = *g;
+  e->have_globals = true;
+  e->graph_valid = false;
+  return VXG_OK;
+}
+
+int vxg_set_nearby(vxg_engine* e, const int* offsets, const int* items, long long n_items) {
+  if (!e || !offsets || (n_items > 0 && !items)) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  int rc = e->col.set_nearby(e->nv, offsets, items, n_items, e->stream);
+  if (rc) return fail(e, rc, "nearby upload");
+  rebuild_view(e);
+  return VXG_OK;
+}
+
+// enqueue one step (no synchronisation); in timing mode `ev` holds this step's 4 events
+static void enqueue_step(vxg_engine* e, float dt, int parity, cudaEvent_t* ev = nullptr) {
+  const View& S = e->S;
+  bool rec = dt < 0;
+  if (ev) cudaEventRecord(ev[0], e->stream);
+  if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S);
+  if (e->nl) {
+    if (rec) k_link<true, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(S, parity);
+    else k_link<false, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(S, parity);
+  }
+  if (ev) cudaEventRecord(ev[1], e->stream);
+  if (e->g.collisions) e->col.enqueue(e->g, e->stream);
+  if (ev) cudaEventRecord(ev[2], e->stream);
+  if (rec) k_voxel<true><<<grid_for(e->nv), kBlock, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+  else k_voxel<false><<<grid_for(e->nv), kBlock, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+  if (ev) cudaEventRecord(ev[3], e->stream);
+}
+
+int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged) {
+  if (!e || nsteps < 0) return VXG_E_ARG;
+  if (!e->have_globals) return fail(e, VXG_E_STATE, "vxg_set_globals was not called");
+  if (steps_done) *steps_done = 0;
+  if (diverged) *diverged = 0;
+  if (nsteps == 0 || dt == 0.0f) {
+    if (steps_done) *steps_done = nsteps;
+    return VXG_OK;
+  }
+  VXG_CK(cudaSetDevice(e->device));
+  // reset the per-batch control words (keep time and counters)
+  int zeros[4] = {0, 0, 0, 0};
+  VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
+  unsigned z2[2] = {0u, 0u};
+  VXG_CK(cudaMemcpyAsync(e->ctl->maxf, z2, sizeof(z2), cudaMemcpyHostToDevice, e->stream));
+  bool use_graph = !e->timing && nsteps > 1;
+  e->tev_used = 0;
+  if (use_graph) {
+    if (!e->graph_valid || e->graph_n != nsteps || e->graph_dt != dt) {
+      if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+      cudaGraph_t g;
+      VXG_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+      for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1);
+      VXG_CK(cudaStreamEndCapture(e->stream, &g));
+      cudaError_t c = cudaGraphInstantiate(&e->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (c != cudaSuccess) return fail(e, VXG_E_CUDA, "graph instantiate", c);
+      e->graph_n = nsteps;
+      e->graph_dt = dt;
+      e->graph_valid = true;
+    }
+    VXG_CK(cudaGraphLaunch(e->graph, e->stream));
+  } else if (e->timing) {
+    size_t need = (size_t)4 * nsteps;
+    while (e->tev.size() < need) {
+      cudaEvent_t x;
+      VXG_CK(cudaEventCreate(&x));
+      e->tev.push_back(x);
+    }
+    for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, &e->tev[(size_t)4 * s]);
+    e->tev_used = nsteps;
+  } else {
+    for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1);
+  }
+  int h[4];
+  VXG_CK(cudaMemcpyAsync(h, e->ctl, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  VXG_CK(cudaGetLastError());
+  if (e->timing && e->tev_used > 0) {
+    double a = 0, b = 0, c = 0;
+    for (int s = 0; s < e->tev_used; ++s) {
+      float x = 0, y = 0, z = 0;
+      cudaEvent_t* ev = &e->tev[(size_t)4 * s];
+      cudaEventElapsedTime(&x, ev[0], ev[1]);
+      cudaEventElapsedTime(&y, ev[1], ev[2]);
+      cudaEventElapsedTime(&z, ev[2], ev[3]);
+      a += x; b += y; c += z;
+    }
+    e->t_link = (float)(a / e->tev_used);
+    e->t_col = (float)(b / e->tev_used);
+    e->t_vox = (float)(c / e->tev_used);
+    cudaEventElapsedTime(&e->t_batch, e->tev[0], e->tev[(size_t)4 * (e->tev_used - 1) + 3]);
+  }
+  if (steps_done) *steps_done = h[2];
+  if (diverged) *diverged = h[1] ? 1 : 0;
+  if (h[3]) return fail(e, VXG_E_DEVICE_STATUS, e->col.status_message(h[3]));
+  return VXG_OK;
+}
+
+int vxg_recommended_dt(vxg_engine* e, float* dt) {
+  if (!e || !dt) return VXG_E_ARG;
+  if (!e->have_globals) return fail(e, VXG_E_STATE, "vxg_set_globals was not called");
+  VXG_CK(cudaSetDevice(e->device));
+  int zeros[4] = {0, 0, 0, 0};
+  VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
+  unsigned z = 0u;
+  VXG_CK(cudaMemcpyAsync(&e->ctl->maxf[0], &z, 4, cudaMemcpyHostToDevice, e->stream));
+  if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S);
+  if (e->nl) k_link<true, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S, 0);
+  unsigned u = 0;
+  VXG_CK(cudaMemcpyAsync(&u, &e->ctl->maxf[0], 4, cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  VXG_CK(cudaGetLastError());
+  float mx;
+  std::memcpy(&mx, &u, 4);
+  if (mx <= 0.0f) mx = e->g.fallback_freq2;
+  *dt = (mx <= 0.0f) ? 0.0f : 1.0f / (6.283185f * sqrtf(mx));
+  return VXG_OK;
+}
+
+int vxg_set_all_temperatures(vxg_engine* e, float t) {
+  if (!e) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  if (e->nv) k_set_temp<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S, t);
+  if (e->nl) k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
+  VXG_CK(cudaGetLastError());
+  return VXG_OK;
+}
+
+int vxg_set_temperatures(vxg_engine* e, const float* t) {
+  if (!e || (!t && e->nv)) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  if (e->nv) VXG_CK(cudaMemcpyAsync(e->S.temp, t, sizeof(float) * (size_t)e->nv, cudaMemcpyHostToDevice, e->stream));
+  if (e->nl) k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
+  VXG_CK(cudaGetLastError());
+  return VXG_OK;
+}
+
+int vxg_reduce(vxg_engine* e, int info, int type, float* out) {
+  if (!e || !out || info < 0 || info > 9 || type < 0 || type > 3) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  bool link = info == 5 || info == 6 || info == 7;
+  int n = link ? e->nl : e->nv;
+  if (n == 0) { *out = 0.0f; return VXG_OK; }
+  if (info == 8) return fail(e, VXG_E_ARG, "PRESSURE is reduced on the host");
+  int blocks = std::min(4096, grid_for(n));
+  k_reduce<<<blocks, kBlock, 0, e->stream>>>(e->S, info, n, e->d_partials);
+  std::vector<double> h((size_t)3 * blocks);
+  VXG_CK(cudaMemcpyAsync(h.data(), e->d_partials, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  double mn = h[0], mx = h[1], sm = 0.0;
+  for (int b = 0; b < blocks; ++b) {
+    mn = std::min(mn, h[3 * b]);
+    mx = std::max(mx, h[3 * b + 1]);
+    sm += h[3 * b + 2];
+  }
+  switch (type) {
+    case 0: *out = (float)mn; break;
+    case 1: *out = (float)mx; break;
+    case 2: *out = (float)sm; break;
+    default: *out = (float)(sm / n); break;
+  }
+  return VXG_OK;
+}
+
+int vxg_get_collisions(vxg_engine* e, int* pairs, int cap, int* n) {
+  if (!e || !n) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  int rc = e->col.get_pairs(pairs, cap, n, e->stream);
+  return rc ? fail(e, rc, "collision readback") : VXG_OK;
+}
+
+int vxg_counters(vxg_engine* e, long long* out, int n) {
+  if (!e || !out || n < 0) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  unsigned long long h[VXG_C_COUNT];
+  VXG_CK(cudaMemcpyAsync(h, e->ctl->counters, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  h[VXG_C_REBUILDS] = (unsigned long long)e->col.rebuilds();
+  h[VXG_C_PAIRS] = (unsigned long long)e->col.pairs(e->stream);
+  for (int i = 0; i < n && i < VXG_C_COUNT; ++i) out[i] = (long long)h[i];
+  return VXG_OK;
+}
+
+int vxg_enable_timing(vxg_engine* e, int on) {
+  if (!e) return VXG_E_ARG;
+  e->timing = on != 0;
+  return VXG_OK;
+}
+
+int vxg_last_step_timing(vxg_engine* e, float* a, float* b, float* c) {
+  if (!e) return VXG_E_ARG;
+  if (a) *a = e->t_link;
+  if (b) *b = e->t_col;
+  if (c) *c = e->t_vox;
+  return VXG_OK;
+}
+
+int vxg_last_batch_ms(vxg_engine* e, float* ms) {
+  if (!e || !ms) return VXG_E_ARG;
+  *ms = e->t_batch;
+  return VXG_OK;
+}
+
+const char* vxg_last_error(const vxg_engine* e) { return e ? e->err.c_str() : "null engine"; }
+void* vxg_stream(vxg_engine* e) { return e ? (void*)e->stream : nullptr; }
+int vxg_synchronize(vxg_engine* e) {
+  if (!e) return VXG_E_ARG;
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  return VXG_OK;
+}
+
+}  // extern "C"

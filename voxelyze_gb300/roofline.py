@@ -1,0 +1,35 @@
+"""Algorithmic bytes of one time step, frozen from the device layout of the FP64 and FP32C paths.
+
+Each persistent field a pass touches is counted once read and once written; each gather of a
+voxel field by the link pass is counted once per voxel (not per link end); material tables are not
+counted.  These are the figures bench.py divides by the CUDA-event time of each pass.
+
+FP64 layout (voxelyze_gb300/csrc/vx_phys64.cuh):
+  link pass, per link : endpoint ids 8, flags 4+4, material id 4, previous pos2/angle1v/angle2v 72
+                        read + 72 written, rest length 8, transverse area/strain sum 8, strain /
+                        maxStrain / strainOffset 12 read + strain/maxStrain/strainOffset/stress 16
+                        written, forces and moments 96 written                          = 304 B
+            per voxel : position 24, orientation 32, previous dt 4, material id 4      =  64 B
+  Poisson pre-pass (nu != 0), per voxel: flags 4+4, 6 link ids 24, cached strain 12   =  44 B
+                        (the link strains it gathers are counted once per link: 8 B)
+  voxel pass, per voxel: pose and momenta 104 read + 104 written, flags 4+4, material id 4,
+                        external id 4, 6 link ids 24, lattice index 12, temperature 4,
+                        previous dt 4 written                                          = 268 B
+            per link  : the force and moment each end gathers, 2 x 48                 =  96 B
+"""
+from __future__ import annotations
+
+FP64_LINK_PER_LINK = 304
+FP64_LINK_PER_VOXEL = 64
+FP64_POISSON_PER_VOXEL = 44
+FP64_POISSON_PER_LINK = 8
+FP64_VOXEL_PER_VOXEL = 268
+FP64_VOXEL_PER_LINK = 96
+
+
+def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
+    link = FP64_LINK_PER_LINK * n_links + FP64_LINK_PER_VOXEL * n_voxels
+    if poisson:
+        link += FP64_POISSON_PER_VOXEL * n_voxels + FP64_POISSON_PER_LINK * n_links
+    voxel = FP64_VOXEL_PER_VOXEL * n_voxels + FP64_VOXEL_PER_LINK * n_links
+    return {"link": link, "voxel": voxel, "step": link + voxel}
