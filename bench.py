@@ -1,16 +1,18 @@
 #!/usr/bin/env python
 """Time-step throughput of the GB300 engine on the 128x128x64 multi-material lattice.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision fp64|fp32c]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision fp32c|fp64]
 
 Workload (seeded, synthetic; no public dataset exists for this path): 128x128x64 grid, Bernoulli
 0.85 fill (largest 6-connected component kept: ~0.89 M voxels, ~2.25 M links), 4 bilinear
 materials (E log-uniform 1e5..1e7 Pa, rho 1000..3000, nu 0.3), gravity and floor, 1 cm voxels,
 dt = recommendedTimeStep() at t = 0, then fixed.  A bench step is one doTimeStep.
 
-value  voxel-steps/s with the scene resident on the GPU: K steps timed with CUDA events on the
-       engine stream (first to last kernel), max over ranks.  The state (~1 GB) exceeds L2, so no
-       flush is needed between steps.
+value  voxel-steps/s of the FP32-compensated path (--precision, default fp32c) with the scene
+       resident on the GPU: K steps timed with CUDA events on the engine stream (first to last
+       kernel), max over ranks.  The FP64 path is timed the same way in the same run and reported
+       beside it, with the FP32C position error against it (the FP64 path is bit-identical to the
+       FP64 oracle).  The state (0.6-1 GB) exceeds L2, so no flush is needed between steps.
 e2e    the same metric through the public C facade per step: upload every voxel's temperature from
        pinned host memory (vx_set_temperatures), doTimeStep, read every position back into pinned
        memory (vx_read_positions); host wall clock.
@@ -111,10 +113,13 @@ def _traffic(kernel: str, n_voxels: int, n_links: int):
         return None
 
 
+DIMS = (128, 128, 64)
+
+
 def build_lattice(sim_factory):
     from voxelyze_gb300 import scenes as S
 
-    sc = S.lattice(128, 128, 64)
+    sc = S.lattice(*DIMS)
     sim = sim_factory(sc.voxel_size)
     S.apply(sc, sim)
     return sc, sim
@@ -146,7 +151,7 @@ def run_reference(args, world, rank):
         return
     from voxelyze_gb300 import scenes as S
 
-    sc = S.lattice(128, 128, 64)
+    sc = S.lattice(*DIMS)
     cores = os.cpu_count() or 1
     # warmup and timed steps, each one doTimeStep of the full lattice on all host cores
     rate_w, _, _ = cpu_oracle_rate(sc, cores, 0.0, steps_cap=max(1, args.warmup))
@@ -162,8 +167,28 @@ def run_reference(args, world, rank):
     print(json.dumps(line))
 
 
+def _timed(lib, sim, steps, dt, local, barrier):
+    """K steps with per-kernel CUDA events on the engine stream; returns timings and clocks."""
+    h = C.c_void_p(sim.h)
+    lib.vx_enable_timing(h, 1)
+    barrier()
+    with _Clocks(local) as clk:
+        done = sim.do_time_steps(steps, dt)
+    barrier()
+    lib.vx_enable_timing(h, 0)
+    if done != steps:
+        raise RuntimeError(f"diverged after {done} steps")
+    tm = (C.c_float * 4)()
+    lib.vx_step_timing(h, tm)
+    batch_ms, link_ms, col_ms, vox_ms = [float(x) for x in tm]
+    # first kernel to last kernel of the batch, extended by one step's share of the gap
+    total_ms = batch_ms * steps / max(steps - 1, 1) if steps > 1 else link_ms + col_ms + vox_ms
+    return {"total_ms": total_ms, "link_ms": link_ms, "collide_ms": col_ms, "voxel_ms": vox_ms, "clocks": clk.summary()}
+
+
 def run_ours(args, world, rank, local):
     import voxelyze_gb300 as vg
+    from voxelyze_gb300 import roofline as R
 
     if world > 1:
         import torch
@@ -171,17 +196,6 @@ def run_ours(args, world, rank, local):
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    lib = vg.library()
-    sc, sim = build_lattice(vg.Sim)
-    nv, nl = sim.voxel_count(), sim.link_count()
-    if args.precision == "fp32c":
-        if lib.vx_set_precision(C.c_void_p(sim.h), 1) != 0:
-            raise RuntimeError("FP32C precision not available")
-    dt = sim.recommended_time_step()
-    h = C.c_void_p(sim.h)
-    lib.vx_step_timing.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
-    if sim.do_time_steps(args.warmup, dt) != args.warmup:
-        raise RuntimeError("warm-up diverged")
 
     def barrier():
         if world > 1:
@@ -189,32 +203,48 @@ def run_ours(args, world, rank, local):
 
             dist.barrier()
 
-    # ---- device-timed throughput (CUDA events on the engine stream) -------------------------
-    lib.vx_enable_timing(h, 1)
-    barrier()
-    with _Clocks(local) as clk:
-        done = sim.do_time_steps(args.steps, dt)
-    barrier()
-    lib.vx_enable_timing(h, 0)
-    if done != args.steps:
-        raise RuntimeError(f"diverged after {done} steps")
-    tm = (C.c_float * 4)()
-    lib.vx_step_timing(h, tm)
-    batch_ms, link_ms, col_ms, vox_ms = [float(x) for x in tm]
-    # per-step time over the timed region: first kernel to last, plus one step's own length
-    total_ms = batch_ms * args.steps / max(args.steps - 1, 1) if args.steps > 1 else link_ms + col_ms + vox_ms
-    if world > 1:
+    def max_over_ranks(x):
+        if world == 1:
+            return x
         import torch
         import torch.distributed as dist
 
-        t = torch.tensor([total_ms], device="cuda")
+        t = torch.tensor([x], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * nv * args.steps / (total_ms / 1e3)
+        return float(t.item())
+
+    lib = vg.library()
+    lib.vx_step_timing.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+    sc, sim64 = build_lattice(vg.Sim)
+    _, sim32 = build_lattice(vg.Sim)
+    if lib.vx_set_precision(C.c_void_p(sim32.h), 1) != 0:
+        raise RuntimeError("FP32C precision not available")
+    nv, nl = sim64.voxel_count(), sim64.link_count()
+    dt = sim64.recommended_time_step()
+    sim32.recommended_time_step()
+    for sim in (sim64, sim32):
+        if sim.do_time_steps(args.warmup, dt) != args.warmup:
+            raise RuntimeError("warm-up diverged")
+    head = sim32 if args.precision == "fp32c" else sim64
+    other = sim64 if head is sim32 else sim32
+    t_head = _timed(lib, head, args.steps, dt, local, barrier)
+    t_other = _timed(lib, other, args.steps, dt, local, barrier)
+    for t in (t_head, t_other):
+        t["total_ms"] = max_over_ranks(t["total_ms"])
+        t["value"] = world * nv * args.steps / (t["total_ms"] / 1e3)
+
+    # FP32C error against the FP64 path (bit-identical to the FP64 oracle) after the same steps
+    p64 = sim64.voxel_state()["pos"]
+    p32 = sim32.voxel_state()["pos"]
+    disp = p64 - sc.xyz * sc.voxel_size
+    err = {"steps": args.warmup + args.steps,
+           "rel_pos": float(np.abs(p32 - p64).max() / np.abs(p64).max()),
+           "rel_disp": float(np.abs(p32 - p64).max() / max(np.abs(disp).max(), 1e-30))}
 
     # ---- end to end through the public C facade ----------------------------------------------
     import torch
 
+    h = C.c_void_p(head.h)
     temps = torch.zeros(nv, dtype=torch.float32, pin_memory=True)
     pos = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
     lib.vx_set_temperatures.argtypes = [C.c_void_p, C.c_void_p]
@@ -229,25 +259,24 @@ def run_ours(args, world, rank, local):
             raise RuntimeError("e2e step diverged")
         if lib.vx_read_positions(h, pos.data_ptr()) != 0:
             raise RuntimeError("vx_read_positions failed")
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
     barrier()
     e2e_value = world * nv * e2e_steps / e2e_s
 
-    # ---- roofline of the dominant pass -----------------------------------------------------
-    from voxelyze_gb300 import roofline as R
-
-    b = R.fp64_bytes(nv, nl, poisson=True)
-    kernel = "link" if link_ms >= vox_ms else "voxel"
-    k_ms = link_ms if kernel == "link" else vox_ms
+    # ---- roofline of the dominant pass of the headline precision ------------------------------
+    fp32 = head is sim32
+    b = (R.fp32c_bytes if fp32 else R.fp64_bytes)(nv, nl, poisson=True)
+    kernel = "link" if t_head["link_ms"] >= t_head["voxel_ms"] else "voxel"
+    k_ms = t_head[f"{kernel}_ms"]
     achieved = b[kernel] / (k_ms / 1e3) / 1e9
     peak, peak_kind = _peak_hbm()
-    roof = {"bound": "hbm", "kernel": f"k_{kernel} (FP64 {kernel} pass)", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+    kname = f"k_{kernel}{'32' if fp32 else ''}"
+    roof = {"bound": "hbm", "kernel": f"{kname} ({'FP32C' if fp32 else 'FP64'} {kernel} pass)", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": b[kernel], "ms_per_launch": k_ms,
-            "traffic": _traffic(f"k_{kernel}_fp64", nv, nl),
-            "note": "FP64 pass: bound by the FP64 pipe on GB300, not by HBM"}
+            "traffic": _traffic(f"{kname}_{'fp32c' if fp32 else 'fp64'}", nv, nl),
+            "step_bytes": b["step"], "step_frac": b["step"] / (t_head["total_ms"] / args.steps / 1e3) / 1e9 / peak}
 
-    # ---- CPU baseline: the oracle on the host cores, bounded sample ----------------------------
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
@@ -255,19 +284,23 @@ def run_ours(args, world, rank, local):
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{n} doTimeStep calls of the full lattice in {el:.1f} s (OpenMP, C-library math)"}
 
-    launches_per_step = 3  # Poisson pre-pass, link pass, voxel pass
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
-            "data": "synthetic",
-            "config": {"workload": "lattice 128x128x64, fill 0.85, 4 bilinear materials, nu 0.3, gravity+floor, 1 cm",
+    o = t_other
+    line = {"metric": METRIC, "value": t_head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_head["total_ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if fp32 else "f64", "data": "synthetic",
+            "config": {"workload": "lattice %dx%dx%d, fill 0.85, 4 bilinear materials, nu 0.3, gravity+floor, 1 cm" % DIMS,
                        "voxels": nv, "links": nl, "precision": args.precision, "parallelism": f"replicas x{world}",
-                       "l2": "state ~1 GB > 129 MB L2, no flush", "dt": dt,
-                       "per_pass_ms": {"link": link_ms, "collide": col_ms, "voxel": vox_ms}},
+                       "l2": "state > 129 MB L2 (FP64 ~1 GB, FP32C ~0.6 GB), no flush", "dt": dt,
+                       "per_pass_ms": {"link": t_head["link_ms"], "voxel": t_head["voxel_ms"]},
+                       "other_precision": {"precision": "fp64" if fp32 else "fp32c", "value": o["value"],
+                                           "ms_per_step": o["total_ms"] / args.steps,
+                                           "per_pass_ms": {"link": o["link_ms"], "voxel": o["voxel_ms"]}},
+                       "fp32c_over_fp64": (t_head["value"] / o["value"]) if fp32 else (o["value"] / t_head["value"]),
+                       "fp32c_error_vs_fp64": err},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * nv, "d2h_bytes_per_step": 24 * nv,
                     "steps": e2e_steps},
-            "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps}
+            "clocks": t_head["clocks"], "gpu_launches": 3 * args.steps}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -282,10 +315,13 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"])
+    ap.add_argument("--precision", default="fp32c", choices=["fp64", "fp32c"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--dims", default="128,128,64", help="lattice size (smaller cases for profiling)")
     args = ap.parse_args()
+    global DIMS
+    DIMS = tuple(int(x) for x in args.dims.split(","))
     world, rank, local = _dist()
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -1,0 +1,99 @@
+"""FP32-compensated path (precision mode 1) against the FP64 path.
+
+The FP64 GPU path is bit-identical to the oracle (test_gpu_parity.py), so its positions stand in
+for the FP64 oracle here.  Errors are stated as
+    max |pos_fp32c - pos_fp64| / max |pos_fp64|        (relative position error)
+    max |pos_fp32c - pos_fp64| / max |disp_fp64|       (relative to the largest displacement)
+and each test states its tolerance.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import make_sim
+from voxelyze_gb300 import facade as F, scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(product_lib, scene):
+    a = make_sim(product_lib, "vx", scene)
+    b = make_sim(product_lib, "vx", scene)
+    assert product_lib.vx_set_precision(__import__("ctypes").c_void_p(b.h), 1) == 0
+    return a, b
+
+
+def _errors(a, b, scene):
+    pa, pb = a.voxel_state()["pos"], b.voxel_state()["pos"]
+    disp = pa - scene.xyz * scene.voxel_size
+    d = np.abs(pa - pb)
+    return float(d.max() / np.abs(pa).max()), float(d.max() / max(np.abs(disp).max(), 1e-30))
+
+
+def test_lattice_1000_steps(product_lib):
+    """The 128x128x64 multi-material lattice, 1,000 steps: relative position error <= 1e-5."""
+    sc = S.lattice(128, 128, 64)
+    a, b = _pair(product_lib, sc)
+    dt = a.recommended_time_step()
+    assert b.recommended_time_step() == pytest.approx(dt, rel=1e-6)
+    assert a.do_time_steps(1000, dt) == 1000
+    assert b.do_time_steps(1000, dt) == 1000
+    rel_pos, rel_disp = _errors(a, b, sc)
+    print(f"lattice 128x128x64, 1000 steps: rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
+    assert rel_pos <= 1e-5
+    assert rel_disp <= 1e-2
+
+
+def test_small_lattice_poisson_dt_every_step(product_lib):
+    sc = S.lattice(16, 16, 8)
+    a, b = _pair(product_lib, sc)
+    assert a.do_time_steps(300, -1.0) == 300
+    assert b.do_time_steps(300, -1.0) == 300
+    rel_pos, rel_disp = _errors(a, b, sc)
+    print(f"lattice 16x16x8, dt every step, 300 steps: rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
+    assert rel_pos <= 1e-5
+
+
+def test_population_with_temperature(product_lib):
+    sc = S.population(16, 4, 10)
+    a, b = _pair(product_lib, sc)
+    dt = a.recommended_time_step()
+    b.recommended_time_step()
+    for k in range(10):
+        t = 0.1 * np.sin(2 * np.pi * 2 * k * 50 * dt)
+        a.set_ambient_temperature(float(t), True)
+        b.set_ambient_temperature(float(t), True)
+        assert a.do_time_steps(50, dt) == 50
+        assert b.do_time_steps(50, dt) == 50
+    rel_pos, rel_disp = _errors(a, b, sc)
+    print(f"population 16 bodies, CTE actuation, 500 steps: rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
+    assert rel_pos <= 1e-5
+
+
+def test_cantilever_small_deflection(product_lib):
+    """Static-like cantilever (small load): FP32C converges to the same deflection."""
+    sc = S.cantilever(20, 4, 4, voxel_size=0.005, tip_force=-0.01)
+    a, b = _pair(product_lib, sc)
+    dt = a.recommended_time_step()
+    b.recommended_time_step()
+    assert a.do_time_steps(3000, dt) == 3000
+    assert b.do_time_steps(3000, dt) == 3000
+    rel_pos, rel_disp = _errors(a, b, sc)
+    print(f"cantilever 20x4x4, 3000 steps: rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
+    assert rel_pos <= 1e-5
+    assert rel_disp <= 1e-3
+
+
+def test_fp32c_state_roundtrip_and_reset(product_lib):
+    sc = S.lattice(8, 8, 4)
+    a, b = _pair(product_lib, sc)
+    dt = a.recommended_time_step()
+    b.recommended_time_step()
+    b.do_time_steps(100, dt)
+    b.reset_time()
+    a.reset_time()
+    st_a, st_b = a.voxel_state(), b.voxel_state()
+    assert np.array_equal(st_a["pos"], st_b["pos"])
+    assert b.do_time_steps(50, dt) == 50
+    assert np.all(np.isfinite(b.voxel_state()["pos"]))

@@ -1,0 +1,143 @@
+"""Pins the oracle to the reference.
+
+1. Golden fixtures (tests/golden, made by tests/golden/make_golden.py from the reference library
+   compiled from its own sources): the oracle in its C-library mode must reproduce every digest
+   bit for bit on the platform the fixtures were made on.  On another platform the C library's
+   sin/cos/acos/powf may round differently, so there the sampled states are compared to 1e-9.
+2. The live reference build (oracle/_ref, only where the reference sources exist): bit-identical
+   state after every checkpoint on a set of scenes covering every branch of the time step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import platform
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, make_sim, state_diff
+from voxelyze_gb300 import facade as F, scenes as S
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, GOLDEN)
+from make_golden import SCENES, digest, snapshot  # noqa: E402
+
+META = json.load(open(os.path.join(GOLDEN, "golden.json")))
+
+
+@pytest.mark.parametrize("name", sorted(META["scenes"]))
+def test_oracle_reproduces_golden(oracle_lib, name):
+    oracle_lib.vxo_set_math(0)
+    entry = META["scenes"][name]
+    mk, steps, cps, mode, full = SCENES[name]
+    sc = mk()
+    sim = make_sim(oracle_lib, "vxo", sc)
+    assert (sim.voxel_count(), sim.link_count()) == (entry["n_voxels"], entry["n_links"])
+    dt = sim.recommended_time_step()
+    assert dt == entry["dt"]
+    use = -1.0 if mode == "every_step" else dt
+    same_platform = platform.machine() == META["platform"]
+    arrays = np.load(os.path.join(GOLDEN, f"{name}.npz")) if os.path.exists(os.path.join(GOLDEN, f"{name}.npz")) else None
+    sample = np.array(entry["sample"])
+    for k, cp in enumerate(entry["checkpoints"]):
+        assert sim.do_time_steps(steps, use) == steps
+        snap, _ = snapshot(sim, False, None)
+        if same_platform:
+            for key in ("voxel_d", "voxel_f", "voxel_i", "link_d", "link_f", "link_i"):
+                assert snap[key] == cp[key], (name, k, key)
+            if "pairs" in cp:
+                assert digest(sim.collisions().astype(np.int32)) == cp["pairs"]
+        elif arrays is not None:
+            key = f"cp{k}_voxel_d_sample" if f"cp{k}_voxel_d_sample" in arrays else f"cp{k}_voxel_d"
+            ref = arrays[key]
+            got = sim.voxel_state()["raw_d"][sample] if "sample" in key else sim.voxel_state()["raw_d"]
+            scale = np.max(np.abs(ref[:, :3]))
+            assert np.max(np.abs(got[:, :3] - ref[:, :3])) <= 1e-9 * scale
+
+
+SCENES_LIVE = [
+    ("cantilever_full", lambda: S.cantilever(), [200, 800], "fixed"),
+    ("lattice_poisson", lambda: S.lattice(12, 12, 8), [50, 50], "fixed"),
+    ("lattice_dt_every_step", lambda: S.lattice(8, 8, 6, seed=5), [20, 20], "every"),
+    ("porous_collisions", lambda: S.porous(14, sigma=1.2), [100, 150], "fixed"),
+    ("population", lambda: S.population(6, 3, 6), [100], "fixed"),
+]
+
+
+@pytest.mark.parametrize("name,mk,chunks,mode", SCENES_LIVE, ids=[s[0] for s in SCENES_LIVE])
+def test_oracle_matches_live_reference(oracle_lib, ref_lib, name, mk, chunks, mode):
+    oracle_lib.vxo_set_math(0)
+    sc = mk()
+    a = make_sim(ref_lib, "vxr", sc)
+    b = make_sim(oracle_lib, "vxo", sc)
+    assert state_diff(a, b) == []
+    dt = a.recommended_time_step()
+    assert dt == b.recommended_time_step()
+    use = -1.0 if mode == "every" else dt
+    for n in chunks:
+        assert a.do_time_steps(n, use) == b.do_time_steps(n, use)
+        assert state_diff(a, b) == []
+        if sc.collisions:
+            assert np.array_equal(a.collisions(), b.collisions())
+    assert a.current_time() == b.current_time()
+
+
+def _custom(s):
+    m = s.add_material(1e6, 1e3)
+    s.material_set(m, F.PROP_ZETA_GLOBAL, 0.1)
+    s.material_set(m, F.PROP_POISSON, 0.3)
+    m2 = s.add_material(3e6, 1.5e3)
+    s.set_model(m2, [0.01, 0.05, 0.2], [3e4, 8e4, 1.2e5])
+    s.material_set(m2, F.PROP_CTE, 0.01)
+    for i in range(6):
+        for j in range(3):
+            for k in range(2):
+                v = s.set_voxel(m if (i + j) % 2 else m2, i, j, k)
+                if i == 0:
+                    s.set_fixed(v, F.X_TRANSLATE | F.Z_TRANSLATE | F.X_ROTATE)
+                if i == 5:
+                    s.set_displacement(v, F.Y_ROTATE, 0.2)
+                    s.set_moment(v, 1e-4, 0, 2e-4)
+                    s.set_force(v, 0.05, 0.02, -0.1)
+    s.set_gravity(0.5)
+    s.enable_floor(True)
+    s.set_temperature(3, 2.0)
+
+
+def test_oracle_matches_live_reference_edge_features(oracle_lib, ref_lib):
+    """Partial fixes, prescribed rotation, external moments, data-table material, CTE,
+    per-voxel temperature, ambient temperature, reset and every stateInfo reduction."""
+    oracle_lib.vxo_set_math(0)
+    a = F.Sim(ref_lib, "vxr", 0.002)
+    b = F.Sim(oracle_lib, "vxo", 0.002)
+    _custom(a)
+    _custom(b)
+    assert state_diff(a, b) == []
+    for _ in range(3):
+        assert a.do_time_steps(100, -1.0) == b.do_time_steps(100, -1.0)
+        assert state_diff(a, b) == []
+    a.set_ambient_temperature(0.3, True)
+    b.set_ambient_temperature(0.3, True)
+    assert a.do_time_steps(50, -1.0) == b.do_time_steps(50, -1.0)
+    assert state_diff(a, b) == []
+    for info in range(10):
+        for t in range(4):
+            x, y = a.state_info(info, t), b.state_info(info, t)
+            assert x == y or (np.isnan(x) and np.isnan(y)), (info, t, x, y)
+    a.reset_time()
+    b.reset_time()
+    assert state_diff(a, b) == []
+    assert a.do_time_steps(80, -1.0) == b.do_time_steps(80, -1.0)
+    assert state_diff(a, b) == []
+
+
+def test_reference_two_stale_constants(ref_lib):
+    """The two reference KATs with stale expectations: the reference build's own values."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from kats import poissons_small
+
+    r = poissons_small(lambda sz: F.Sim(ref_lib, "vxr", sz))
+    assert abs(float(np.float32(r["x"])) - 1.8513450e-6) < 2e-12

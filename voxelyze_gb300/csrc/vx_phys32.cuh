@@ -1,0 +1,419 @@
+// FP32-compensated time step (precision mode VXG_FP32C).
+//
+// Same algorithm and branch structure as the FP64 path (vx_phys64.cuh, which cites the reference
+// routine by routine), with the bulk arithmetic in FP32 and accuracy won back where FP32 alone
+// would lose it:
+//   * position = exact lattice origin (ix, iy, iz) * voxel size + FP32 displacement d, updated each
+//     step with Kahan compensation (true displacement = d - c);
+//   * the link's relative pose is formed from displacement differences, never from absolute
+//     positions; its axial extension is written so that no two nearly equal numbers are
+//     subtracted: pos2.x - L = -2 s (y^2 + z^2) + (R d).x - (L - s) in the small-angle branch and
+//     (|pos2|^2 - s^2) / (|pos2| + s) - (L - s) in the large-angle one, with the rest length held
+//     as its offset from the nominal size (L - s, exactly 0 at zero temperature);
+//   * link pose and rotation vectors are small quantities stored as such (extension, not length).
+// Transcendental functions are the CUDA single-precision ones.  Errors against the FP64 path are
+// measured, not bounded: tests/test_gpu_fp32c.py reports them per workload.
+#pragma once
+#include <cmath>
+#include <cstdint>
+
+#include "vx_phys64.cuh"
+
+namespace vx32 {
+
+struct f3 {
+  float x, y, z;
+};
+struct q4 {
+  float w, x, y, z;
+};
+VX_HD f3 F3(float a, float b, float c) { f3 r; r.x = a; r.y = b; r.z = c; return r; }
+VX_HD q4 Q4(float w, float x, float y, float z) { q4 q; q.w = w; q.x = x; q.y = y; q.z = z; return q; }
+
+// FP32 working state; everything else (topology, flags, float strain/temperature fields,
+// materials, externals, control block) is the FP64 View's.
+struct View {
+  vx64::View B;     // shared arrays
+  float* d;         // 3 nv displacement from the lattice origin
+  float* c;         // 3 nv Kahan compensation (true displacement = d - c)
+  float* q;         // 4 nv orientation
+  float* lin;       // 3 nv linear momentum
+  float* ang;       // 3 nv angular momentum
+  float* pos2;      // 3 nl (x holds the extension pos2.x - L, as in the reference's state)
+  float* a1v;       // 3 nl
+  float* a2v;       // 3 nl
+  float* fN;        // 3 nl
+  float* fP;
+  float* mN;
+  float* mP;
+  float* restDelta; // nl: rest length - nominal size
+  float s;          // nominal voxel size
+};
+
+VX_HD f3 ld3(const float* p, int n, int i) { return F3(p[i], p[n + i], p[2 * n + i]); }
+VX_HD void st3(float* p, int n, int i, const f3& v) { p[i] = v.x; p[n + i] = v.y; p[2 * n + i] = v.z; }
+VX_HD q4 ldq(const float* p, int n, int i) { return Q4(p[i], p[n + i], p[2 * n + i], p[3 * n + i]); }
+VX_HD void stq(float* p, int n, int i, const q4& q) { p[i] = q.w; p[n + i] = q.x; p[2 * n + i] = q.y; p[3 * n + i] = q.z; }
+
+VX_HD f3 rotate(const q4& q, const f3& f) {
+  float tw = f.x * q.x + f.y * q.y + f.z * q.z;
+  float tx = f.x * q.w - f.y * q.z + f.z * q.y;
+  float ty = f.x * q.z + f.y * q.w - f.z * q.x;
+  float tz = -f.x * q.y + f.y * q.x + f.z * q.w;
+  return F3(q.w * tx + q.x * tw + q.y * tz - q.z * ty, q.w * ty - q.x * tz + q.y * tw + q.z * tx,
+            q.w * tz + q.x * ty - q.y * tx + q.z * tw);
+}
+VX_HD f3 rotate_inv(const q4& q, const f3& f) {
+  float tw = q.x * f.x + q.y * f.y + q.z * f.z;
+  float tx = q.w * f.x - q.y * f.z + q.z * f.y;
+  float ty = q.w * f.y + q.x * f.z - q.z * f.x;
+  float tz = q.w * f.z - q.x * f.y + q.y * f.x;
+  return F3(tw * q.x + tx * q.w + ty * q.z - tz * q.y, tw * q.y - tx * q.z + ty * q.w + tz * q.x,
+            tw * q.z + tx * q.y - ty * q.x + tz * q.w);
+}
+VX_HD q4 qmul(const q4& a, const q4& f) {
+  return Q4(a.w * f.w - a.x * f.x - a.y * f.y - a.z * f.z, a.w * f.x + a.x * f.w + a.y * f.z - a.z * f.y,
+            a.w * f.y - a.x * f.z + a.y * f.w + a.z * f.x, a.w * f.z + a.x * f.y - a.y * f.x + a.z * f.w);
+}
+VX_HD f3 to_rotation_vector(const q4& q) {
+  if (q.w >= 1.0f || q.w <= -1.0f) return F3(0, 0, 0);
+  // 1 - w^2 from the vector part: no cancellation for w close to 1
+  float sl = q.x * q.x + q.y * q.y + q.z * q.z;
+  if (sl <= 0.0f) return F3(0, 0, 0);
+  float vl = sqrtf(sl);
+  float ang = 2.0f * atan2f(vl, q.w);  // same angle as 2 acos(w) on a unit quaternion
+  float k = ang / vl;
+  return F3(k * q.x, k * q.y, k * q.z);
+}
+VX_HD q4 from_rotation_vector(const f3& in) {
+  f3 th = F3(0.5f * in.x, 0.5f * in.y, 0.5f * in.z);
+  float m2 = th.x * th.x + th.y * th.y + th.z * th.z;
+  float w, s;
+  if (m2 < 1e-6f) {  // Taylor terms beyond m^4 are below FP32 resolution here
+    w = 1.0f - 0.5f * m2 + m2 * m2 * (1.0f / 24.0f);
+    s = 1.0f - m2 * (1.0f / 6.0f) + m2 * m2 * (1.0f / 120.0f);
+  } else {
+    float m = sqrtf(m2);
+    w = cosf(m);
+    s = sinf(m) / m;
+  }
+  return Q4(w, th.x * s, th.y * s, th.z * s);
+}
+VX_HD void from_angle_to_pos_x(q4& q, const f3& r) {
+  if (r.x == 0 && r.y == 0 && r.z == 0) return;
+  float yx = r.y / r.x, zx = r.z / r.x;
+  if (yx < 1.732e-2f && yx > -1.732e-2f && zx < 1.732e-2f && zx > -1.732e-2f) {
+    q.x = 0;
+    q.y = 0.5f * zx;
+    q.z = -0.5f * yx;
+    q.w = 1 + 0.5f * (-q.y * q.y - q.z * q.z);
+    return;
+  }
+  float l = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
+  f3 n = F3(r.x / l, r.y / l, r.z / l);
+  float t = sqrtf(n.z * n.z + n.y * n.y);
+  float theta = atan2f(t, n.x);
+  if (theta > 3.14159265358979f - 1e-7f) {
+    q = Q4(0, 0, 1, 0);
+    return;
+  }
+  float a = 0.5f * theta;
+  float s = sinf(a) / t;
+  q.w = cosf(a);
+  q.x = 0;
+  q.y = n.z * s;
+  q.z = -n.y * s;
+}
+VX_HD f3 to_axis_x(int axis, const f3& v) { return axis == 1 ? F3(v.y, -v.x, v.z) : (axis == 2 ? F3(v.z, v.y, -v.x) : v); }
+VX_HD q4 to_axis_x(int axis, const q4& q) { return axis == 1 ? Q4(q.w, q.y, -q.x, q.z) : (axis == 2 ? Q4(q.w, q.z, q.y, -q.x) : q); }
+VX_HD f3 to_axis_original(int axis, const f3& v) { return axis == 1 ? F3(-v.y, v.x, v.z) : (axis == 2 ? F3(-v.z, v.y, v.x) : v); }
+
+// rest length offset L - s of a link from the two voxels' temperatures (CTE expansion)
+VX_HD float rest_delta(const View& S, int vn, int vp, int axis) {
+  const vxg_voxel_material& a = S.B.vm[S.B.vmat[vn]];
+  const vxg_voxel_material& b = S.B.vm[S.B.vmat[vp]];
+  float ea = (float)a.size[axis] * (S.B.temp[vn] * a.alphaCTE) + ((float)a.size[axis] - S.s);
+  float eb = (float)b.size[axis] * (S.B.temp[vp] * b.alphaCTE) + ((float)b.size[axis] - S.s);
+  return 0.5f * (ea + eb);
+}
+
+VX_HD float link_freq2(const View& S, int l, int vn, int vp, int axis, const vxg_link_material& m) {
+  float k;
+  if (m.nu == 0.0f) {
+    k = m.a1;
+  } else {
+    float rd = rest_delta(S, vn, vp, axis);
+    float ta = 0.5f * (vx64::transverse_area(S.B, vn, axis) + vx64::transverse_area(S.B, vp, axis));
+    float ts = 0.5f * (vx64::transverse_strain_sum(S.B, vn, axis) + vx64::transverse_strain_sum(S.B, vp, axis));
+    S.restDelta[l] = rd;
+    S.B.tArea[l] = ta;
+    S.B.tSS[l] = ts;
+    k = m.eHat * ta / ((S.B.strain[l] + 1) * (S.s + rd));
+  }
+  float m1 = S.B.vm[S.B.vmat[vn]].mass, m2 = S.B.vm[S.B.vmat[vp]].mass;
+  return k / (m1 < m2 ? m1 : m2);
+}
+
+VX_HDN void link_update(const View& S, int l) {
+  const vx64::View& B = S.B;
+  const int nl = B.nl, nv = B.nv;
+  uint32_t lf = B.lflags[l];
+  int axis = (lf >> 8) & 3;
+  bool smallAngle = lf & VXG_LF_SMALL_ANGLE;
+  bool lvv = lf & VXG_LF_LOCAL_VEL_VALID;
+  int vn = B.lvox[l], vp = B.lvox[nl + l];
+  const vxg_link_material& m = B.lm[B.lmat[l]];
+  const float s = S.s;
+  float rd = S.restDelta[l];
+  float L = s + rd;
+
+  f3 oldPos2 = ld3(S.pos2, nl, l), oldA1 = ld3(S.a1v, nl, l), oldA2 = ld3(S.a2v, nl, l);
+  f3 dn = ld3(S.d, nv, vn), dp = ld3(S.d, nv, vp);
+  f3 del = to_axis_x(axis, F3(dp.x - dn.x, dp.y - dn.y, dp.z - dn.z));
+  q4 a1 = to_axis_x(axis, ldq(S.q, nv, vn));
+  q4 a2 = to_axis_x(axis, ldq(S.q, nv, vp));
+  q4 tr = Q4(a1.w, -a1.x, -a1.y, -a1.z);
+  f3 r = rotate(tr, del);
+  // pos2 = s * R e_x + R del, R = rotation by tr; the x part is split off to avoid s - s
+  float ex = -2.0f * s * (tr.y * tr.y + tr.z * tr.z) + r.x;  // pos2.x - s
+  float py = 2.0f * s * (tr.x * tr.y + tr.w * tr.z) + r.y;
+  float pz = 2.0f * s * (tr.x * tr.z - tr.w * tr.y) + r.z;
+  q4 angle2 = qmul(tr, a2);
+  q4 angle1 = Q4(1, 0, 0, 0);
+  float px = s + ex;
+  float smallTurn = (fabsf(pz) + fabsf(py)) / px;
+  float extendPerc = fabsf((ex - rd) / L);
+  const float HF = 1.2f, BEND = 0.05f, EXT = 0.50f;
+  if (!smallAngle && smallTurn < BEND && extendPerc < EXT) {
+    smallAngle = true;
+    lvv = false;
+  } else if (smallAngle && (smallTurn > HF * BEND || extendPerc > HF * EXT)) {
+    smallAngle = false;
+    lvv = false;
+  }
+  f3 pos2;
+  if (smallAngle) {
+    pos2 = F3(ex - rd, py, pz);
+  } else {
+    from_angle_to_pos_x(angle1, F3(px, py, pz));
+    angle2 = qmul(angle1, angle2);
+    float len = sqrtf(px * px + py * py + pz * pz);
+    float lms = (ex * (2.0f * s + ex) + py * py + pz * pz) / (len + s);  // |pos2| - s
+    pos2 = F3(lms - rd, 0, 0);
+  }
+  f3 a1v = to_rotation_vector(angle1);
+  f3 a2v = to_rotation_vector(angle2);
+  st3(S.pos2, nl, l, pos2);
+  st3(S.a1v, nl, l, a1v);
+  st3(S.a2v, nl, l, a2v);
+  f3 dPos2 = F3(0.5f * (pos2.x - oldPos2.x), 0.5f * (pos2.y - oldPos2.y), 0.5f * (pos2.z - oldPos2.z));
+  f3 dA1 = F3(0.5f * (a1v.x - oldA1.x), 0.5f * (a1v.y - oldA1.y), 0.5f * (a1v.z - oldA1.z));
+  f3 dA2 = F3(0.5f * (a2v.x - oldA2.x), 0.5f * (a2v.y - oldA2.y), 0.5f * (a2v.z - oldA2.z));
+
+  float tArea = B.tArea[l], tSS = B.tSS[l];
+  if (!(m.nu == 0.0f) || tSS != 0) {
+    tArea = 0.5f * (vx64::transverse_area(B, vn, axis) + vx64::transverse_area(B, vp, axis));
+    tSS = 0.5f * (vx64::transverse_strain_sum(B, vn, axis) + vx64::transverse_strain_sum(B, vp, axis));
+    B.tArea[l] = tArea;
+    B.tSS[l] = tSS;
+  }
+  float axial = pos2.x / L;
+  float maxStrain = B.maxStrain[l], strainOffset = B.strainOffset[l], stress;
+  if (m.linear) {
+    if (axial > maxStrain) maxStrain = axial;
+    stress = vx64::mat_stress(m, axial, tSS, false);
+  } else if (axial > maxStrain) {
+    maxStrain = axial;
+    stress = vx64::mat_stress(m, axial, tSS, false);
+    if (m.nu != 0.0f) strainOffset = maxStrain - vx64::mat_stress(m, axial, 0.0f, false) / (m.eHat * (1 - m.nu));
+    else strainOffset = maxStrain - stress / m.E;
+  } else {
+    float rel = axial - strainOffset;
+    if (m.nu != 0.0f) stress = vx64::mat_stress(m, rel, tSS, true);
+    else stress = m.E * rel;
+  }
+  B.strain[l] = axial;
+  B.maxStrain[l] = maxStrain;
+  B.strainOffset[l] = strainOffset;
+  B.stress[l] = stress;
+
+  f3 fN, fP, mN, mP;
+  if (m.epsilonFail != -1.0f && maxStrain > m.epsilonFail) {
+    fN = fP = mN = mP = F3(0, 0, 0);
+  } else {
+    float b1 = m.b1, b2 = m.b2, b3 = m.b3, a2c = m.a2;
+    fN = F3(stress * tArea, b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
+    fP = F3(-fN.x, -fN.y, -fN.z);
+    mN = F3(a2c * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (2 * a1v.y + a2v.y), b2 * pos2.y - b3 * (2 * a1v.z + a2v.z));
+    mP = F3(a2c * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z));
+    if (lvv) {
+      f3 pc = F3(m.sqA1 * dPos2.x, m.sqB1 * dPos2.y - m.sqB2xFMp * (dA1.z + dA2.z), m.sqB1 * dPos2.z + m.sqB2xFMp * (dA1.y + dA2.y));
+      const vxg_voxel_material& mn = B.vm[B.vmat[vn]];
+      const vxg_voxel_material& mp = B.vm[B.vmat[vp]];
+      float pdt = B.ctl->last_dt;  // every voxel stepped with the same dt last step
+      float dmN = 2 * mn.sqrtMass * mn.zetaInternal / pdt, dmP = 2 * mp.sqrtMass * mp.zetaInternal / pdt;
+      fN.x += dmN * pc.x; fN.y += dmN * pc.y; fN.z += dmN * pc.z;
+      fP.x -= dmP * pc.x; fP.y -= dmP * pc.y; fP.z -= dmP * pc.z;
+      float hN = 0.5f * dmN, hP = 0.5f * dmP;
+      f3 tN = F3(-m.sqA2xIp * (dA2.x - dA1.x), m.sqB2xFMp * dPos2.z + m.sqB3xIp * (2 * dA1.y + dA2.y),
+                 -m.sqB2xFMp * dPos2.y + m.sqB3xIp * (2 * dA1.z + dA2.z));
+      f3 tP = F3(m.sqA2xIp * (dA2.x - dA1.x), m.sqB2xFMp * dPos2.z + m.sqB3xIp * (dA1.y + 2 * dA2.y),
+                 -m.sqB2xFMp * dPos2.y + m.sqB3xIp * (dA1.z + 2 * dA2.z));
+      mN.x -= hN * tN.x; mN.y -= hN * tN.y; mN.z -= hN * tN.z;
+      mP.x -= hP * tP.x; mP.y -= hP * tP.y; mP.z -= hP * tP.z;
+    } else {
+      lvv = true;
+    }
+    if (!smallAngle) {
+      fN = rotate_inv(angle1, fN);
+      mN = rotate_inv(angle1, mN);
+    }
+    fP = rotate_inv(angle2, fP);
+    mP = rotate_inv(angle2, mP);
+    fN = to_axis_original(axis, fN);
+    fP = to_axis_original(axis, fP);
+    mN = to_axis_original(axis, mN);
+    mP = to_axis_original(axis, mP);
+  }
+  st3(S.fN, nl, l, fN);
+  st3(S.fP, nl, l, fP);
+  st3(S.mN, nl, l, mN);
+  st3(S.mP, nl, l, mP);
+  B.lflags[l] = (lf & ~3u) | (smallAngle ? VXG_LF_SMALL_ANGLE : 0u) | (lvv ? VXG_LF_LOCAL_VEL_VALID : 0u);
+}
+
+VX_HD void kahan_add(float& sum, float& comp, float x) {
+  float y = x - comp;
+  float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+VX_HDN void voxel_update(const View& S, int v, float dt) {
+  const vx64::View& B = S.B;
+  const int nv = B.nv, nl = B.nl;
+  if (dt == 0.0f) return;
+  const vxg_voxel_material& m = B.vm[B.vmat[v]];
+  int ei = B.vext[v];
+  const vxg_external* e = ei >= 0 ? &B.ext[ei] : nullptr;
+  if (e && (e->dof & 0x3F) == 0x3F) {
+    st3(S.d, nv, v, F3((float)e->translation[0], (float)e->translation[1], (float)e->translation[2]));
+    st3(S.c, nv, v, F3(0, 0, 0));
+    stq(S.q, nv, v, Q4((float)e->rotq[0], (float)e->rotq[1], (float)e->rotq[2], (float)e->rotq[3]));
+    st3(S.lin, nv, v, F3(0, 0, 0));
+    st3(S.ang, nv, v, F3(0, 0, 0));
+    return;
+  }
+  uint32_t flags = B.vflags[v];
+  f3 d = ld3(S.d, nv, v), c = ld3(S.c, nv, v), lin = ld3(S.lin, nv, v), ang = ld3(S.ang, nv, v);
+  q4 q = ldq(S.q, nv, v);
+  int lk[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) lk[i] = B.vlinks[i * nv + v];
+  f3 F = F3(0, 0, 0);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    if (lk[i] < 0) continue;
+    const float* src = (i & 1) ? S.fP : S.fN;
+    F.x += src[lk[i]]; F.y += src[nl + lk[i]]; F.z += src[2 * nl + lk[i]];
+  }
+  F = rotate(q, F);
+  if (e) { F.x += e->force[0]; F.y += e->force[1]; F.z += e->force[2]; }
+  {
+    float cg = m.zetaGlobal * m.c2xSqMxExS;
+    F.x -= cg * (m.massInv * lin.x);
+    F.y -= cg * (m.massInv * lin.y);
+    F.z -= cg * (m.massInv * lin.z);
+  }
+  F.z += -m.mass * 9.80665f * m.gravMult;
+  f3 fric = F;
+  bool floorOn = flags & VXG_VF_FLOOR;
+  bool staticF = flags & VXG_VF_STATIC_FRICTION;
+  // floor penetration: (base size - nominal)/2 - z, with z = iz s + d.z
+  float expand = (float)((m.size[0] + m.size[1] + m.size[2]) / 3.0) * (1 + B.temp[v] * m.alphaCTE) - (float)m.nomSize;
+  float zorg = (float)B.vidx[2 * nv + v] * S.s;
+  float pen = (0.5f * expand - zorg) - (d.z - c.z);
+  if (floorOn) {
+    if (pen >= 0) {
+      f3 vel = F3(m.massInv * lin.x, m.massInv * lin.y, m.massInv * lin.z);
+      float normal = m.penetrationStiffness * pen;
+      F.z += normal - (m.zetaCollision * m.c2xSqMxExS) * vel.z;
+      if (staticF) {
+        float surf = F.x * F.x + F.y * F.y;
+        float fr = (m.muStatic * normal) * (m.muStatic * normal);
+        if (surf > fr) staticF = false;
+      } else {
+        float k = m.muKinetic * normal;
+        float len = sqrtf(vel.x * vel.x + vel.y * vel.y);
+        if (len > 0) {
+          F.x -= k * (vel.x / len);
+          F.y -= k * (vel.y / len);
+        }
+      }
+    } else {
+      staticF = false;
+    }
+  }
+  fric = F3(F.x - fric.x, F.y - fric.y, F.z - fric.z);
+  lin.x += dt * F.x; lin.y += dt * F.y; lin.z += dt * F.z;
+  float dtm = dt * m.massInv;
+  f3 tr = F3(dtm * lin.x, dtm * lin.y, dtm * lin.z);
+  if (floorOn && pen >= 0) {
+    float work = fric.x * tr.x + fric.y * tr.y;
+    float hKe = 0.5f * m.massInv * (lin.x * lin.x + lin.y * lin.y);
+    if (hKe + work <= 0) staticF = true;
+    if (staticF) {
+      lin.x = lin.y = 0;
+      tr.x = tr.y = 0;
+    }
+  } else {
+    staticF = false;
+  }
+  kahan_add(d.x, c.x, tr.x);
+  kahan_add(d.y, c.y, tr.y);
+  kahan_add(d.z, c.z, tr.z);
+  f3 M = F3(0, 0, 0);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    if (lk[i] < 0) continue;
+    const float* src = (i & 1) ? S.mP : S.mN;
+    M.x += src[lk[i]]; M.y += src[nl + lk[i]]; M.z += src[2 * nl + lk[i]];
+  }
+  M = rotate(q, M);
+  if (e) { M.x += e->moment[0]; M.y += e->moment[1]; M.z += e->moment[2]; }
+  {
+    float cg = m.zetaGlobal * m.c2xSqIxExSxSxS;
+    M.x -= cg * (m.inertiaInv * ang.x);
+    M.y -= cg * (m.inertiaInv * ang.y);
+    M.z -= cg * (m.inertiaInv * ang.z);
+  }
+  ang.x += dt * M.x; ang.y += dt * M.y; ang.z += dt * M.z;
+  float dti = dt * m.inertiaInv;
+  q = qmul(from_rotation_vector(F3(dti * ang.x, dti * ang.y, dti * ang.z)), q);
+  if (e) {
+    if (e->dof & 1) { d.x = (float)e->translation[0]; c.x = 0; lin.x = 0; }
+    if (e->dof & 2) { d.y = (float)e->translation[1]; c.y = 0; lin.y = 0; }
+    if (e->dof & 4) { d.z = (float)e->translation[2]; c.z = 0; lin.z = 0; }
+    if (e->dof & 56) {
+      if ((e->dof & 56) == 56) {
+        q = Q4((float)e->rotq[0], (float)e->rotq[1], (float)e->rotq[2], (float)e->rotq[3]);
+        ang = F3(0, 0, 0);
+      } else {
+        f3 r = to_rotation_vector(q);
+        if (e->dof & 8) { r.x = 0; ang.x = 0; }
+        if (e->dof & 16) { r.y = 0; ang.y = 0; }
+        if (e->dof & 32) { r.z = 0; ang.z = 0; }
+        q = from_rotation_vector(r);
+      }
+    }
+  }
+  st3(S.d, nv, v, d);
+  st3(S.c, nv, v, c);
+  st3(S.lin, nv, v, lin);
+  st3(S.ang, nv, v, ang);
+  stq(S.q, nv, v, q);
+  B.vflags[v] = (flags & ~(uint32_t)VXG_VF_STATIC_FRICTION) | (staticF ? VXG_VF_STATIC_FRICTION : 0u) |
+                VXG_VF_PSTRAIN_INVALID;
+}
+
+}  // namespace vx32

@@ -447,7 +447,7 @@ struct Collide {
     c_insert<<<gv, 256, 0, s>>>(C);
     c_count<<<gv, 256, 0, s>>>(C);
     c_scan<<<1, 1024, 0, s>>>(C);
-    c_fill<<<gv, 128, 0, s>>>(C);
+    c_fill<<<std::max(1, (nv + 127) / 128), 128, 0, s>>>(C);  // 128 threads: 512 B of partners each
     c_watch<<<gv, 256, 0, s>>>(C);
     c_contact<<<grid_pairs, 256, 0, s>>>(C);
   }

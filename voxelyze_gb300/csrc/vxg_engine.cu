@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "vx_phys32.cuh"
 #include "vx_phys64.cuh"
 #include "vxg.h"
 
@@ -189,6 +190,105 @@ __global__ void k_reduce(View S, int info, int n, double* out /* 3 per block: mi
 
 int grid_for(int n) { return std::max(1, (n + kBlock - 1) / kBlock); }
 
+// ---- FP32C kernels ------------------------------------------------------------------------
+template <bool RECOMMEND, bool FORCES>
+__global__ void __launch_bounds__(kBlock) k_link32(vx32::View S, int parity) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (S.B.ctl->halt) return;
+  float f2 = 0.0f;
+  bool live = l < S.B.nl;
+  if (RECOMMEND && live) {
+    uint32_t lf = S.B.lflags[l];
+    int vn = S.B.lvox[l], vp = S.B.lvox[S.B.nl + l];
+    f2 = vx32::link_freq2(S, l, vn, vp, (lf >> 8) & 3, S.B.lm[S.B.lmat[l]]);
+  }
+  if (RECOMMEND) block_max_to(&S.B.ctl->maxf[parity], f2);
+  if (!FORCES || !live) return;
+  vx32::link_update(S, l);
+  if (S.B.strain[l] > 100) S.B.ctl->diverged = 1;
+}
+
+template <bool RECOMMEND>
+__global__ void __launch_bounds__(kBlock) k_voxel32(vx32::View S, float dt_fixed, int parity, float fallback) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (S.B.ctl->halt) return;
+  if (S.B.ctl->diverged) {
+    if (v == 0) S.B.ctl->halt = 1;
+    return;
+  }
+  float dt = step_dt(S.B, RECOMMEND, dt_fixed, parity, fallback);
+  if (v == 0) {
+    S.B.ctl->steps += 1;
+    S.B.ctl->time += dt;
+    S.B.ctl->last_dt = dt;  // the next step's link pass reads it as every voxel's previous dt
+    if (RECOMMEND) S.B.ctl->maxf[parity ^ 1] = 0u;
+  }
+  if (v >= S.B.nv) return;
+  vx32::voxel_update(S, v, dt);
+}
+// FP64 interchange fields -> FP32C working state (on upload) and back (on read)
+__global__ void k_to32(vx32::View S, double s) {
+  const vx64::View& B = S.B;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < B.nv) {
+    for (int k = 0; k < 3; ++k) {
+      double dd = B.pos[k * B.nv + i] - B.vidx[k * B.nv + i] * s;
+      float d = (float)dd;
+      S.d[k * B.nv + i] = d;
+      S.c[k * B.nv + i] = (float)((double)d - dd);
+      S.lin[k * B.nv + i] = (float)B.linMom[k * B.nv + i];
+      S.ang[k * B.nv + i] = (float)B.angMom[k * B.nv + i];
+    }
+    for (int k = 0; k < 4; ++k) S.q[k * B.nv + i] = (float)B.orient[k * B.nv + i];
+    if (i == 0) B.ctl->last_dt = B.prevDt[0];
+  }
+  if (i < B.nl) {
+    for (int k = 0; k < 3; ++k) {
+      int j = k * B.nl + i;
+      S.pos2[j] = (float)B.pos2[j];
+      S.a1v[j] = (float)B.a1v[j];
+      S.a2v[j] = (float)B.a2v[j];
+      S.fN[j] = (float)B.fN[j];
+      S.fP[j] = (float)B.fP[j];
+      S.mN[j] = (float)B.mN[j];
+      S.mP[j] = (float)B.mP[j];
+    }
+    S.restDelta[i] = (float)(B.rest[i] - s);
+  }
+}
+__global__ void k_to64(vx32::View S, double s) {
+  const vx64::View& B = S.B;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < B.nv) {
+    for (int k = 0; k < 3; ++k) {
+      B.pos[k * B.nv + i] = B.vidx[k * B.nv + i] * s + ((double)S.d[k * B.nv + i] - (double)S.c[k * B.nv + i]);
+      B.linMom[k * B.nv + i] = S.lin[k * B.nv + i];
+      B.angMom[k * B.nv + i] = S.ang[k * B.nv + i];
+    }
+    for (int k = 0; k < 4; ++k) B.orient[k * B.nv + i] = S.q[k * B.nv + i];
+    B.prevDt[i] = B.ctl->last_dt;
+  }
+  if (i < B.nl) {
+    for (int k = 0; k < 3; ++k) {
+      int j = k * B.nl + i;
+      B.pos2[j] = S.pos2[j];
+      B.a1v[j] = S.a1v[j];
+      B.a2v[j] = S.a2v[j];
+      B.fN[j] = S.fN[j];
+      B.fP[j] = S.fP[j];
+      B.mN[j] = S.mN[j];
+      B.mP[j] = S.mP[j];
+    }
+    B.rest[i] = s + (double)S.restDelta[i];
+  }
+}
+__global__ void k_rest32(vx32::View S) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= S.B.nl) return;
+  int axis = (S.B.lflags[l] >> 8) & 3;
+  S.restDelta[l] = vx32::rest_delta(S, S.B.lvox[l], S.B.lvox[S.B.nl + l], axis);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -235,6 +335,10 @@ struct vxg_engine {
   size_t arena_bytes = 0;
   void* field_ptr[VXG_F_COUNT] = {};
   View S{};
+  vx32::View V{};          // FP32C working state (precision == VXG_FP32C)
+  char* arena32 = nullptr;
+  bool fp64_dirty = false; // FP64 interchange fields written since the last conversion
+  bool fp32_ahead = false; // FP32C state newer than the FP64 interchange fields
   Ctl* ctl = nullptr;
   vxg_voxel_material* d_vm = nullptr;
   vxg_link_material* d_lm = nullptr;
@@ -277,6 +381,8 @@ static int fail(vxg_engine* e, int code, const char* what, cudaError_t ce = cuda
 
 static void release_arena(vxg_engine* e) {
   if (e->arena) cudaFree(e->arena);
+  if (e->arena32) cudaFree(e->arena32);
+  e->arena32 = nullptr;
   e->arena = nullptr;
   e->arena_bytes = 0;
   std::memset(e->field_ptr, 0, sizeof(e->field_ptr));
@@ -323,7 +429,28 @@ static void rebuild_view(vxg_engine* e) {
   S.powtab = e->d_powtab;
   S.ctl = e->ctl;
   e->col.bind(S);
+  e->V.B = S;
+  e->V.s = (float)e->g.voxSize;
   e->graph_valid = false;
+}
+
+static bool is_state_field(int f) {
+  return f == VXG_F_POS || f == VXG_F_LINMOM || f == VXG_F_ORIENT || f == VXG_F_ANGMOM || f == VXG_F_PREV_DT ||
+         f == VXG_F_POS2 || f == VXG_F_ANGLE1V || f == VXG_F_ANGLE2V || f == VXG_F_FORCE_NEG ||
+         f == VXG_F_FORCE_POS || f == VXG_F_MOMENT_NEG || f == VXG_F_MOMENT_POS || f == VXG_F_REST_LENGTH;
+}
+// FP32C: bring the working state up to date with uploaded FP64 fields, or the reverse
+static void ensure32(vxg_engine* e) {
+  if (e->precision != VXG_FP32C || !e->fp64_dirty) return;
+  int n = std::max(e->nv, e->nl);
+  if (n) k_to32<<<grid_for(n), kBlock, 0, e->stream>>>(e->V, e->g.voxSize);
+  e->fp64_dirty = false;
+}
+static void ensure64(vxg_engine* e) {
+  if (e->precision != VXG_FP32C || !e->fp32_ahead) return;
+  int n = std::max(e->nv, e->nl);
+  if (n) k_to64<<<grid_for(n), kBlock, 0, e->stream>>>(e->V, e->g.voxSize);
+  e->fp32_ahead = false;
 }
 
 template <class T>
@@ -347,7 +474,7 @@ extern "C" {
 int vxg_create(vxg_engine** out, int device, int precision) {
   if (!out) return VXG_E_ARG;
   *out = nullptr;
-  if (precision != VXG_FP64) return VXG_E_ARG;
+  if (precision != VXG_FP64 && precision != VXG_FP32C) return VXG_E_ARG;
   vxg_engine* e = new vxg_engine();
   e->device = device;
   e->precision = precision;
@@ -406,6 +533,19 @@ int vxg_resize(vxg_engine* e, int nv, int nl) {
   VXG_CK(cudaMemsetAsync(e->arena, 0, total, e->stream));
   e->arena_bytes = total;
   for (int f = 0; f < VXG_F_TIME; ++f) e->field_ptr[f] = e->arena + off[f];
+  if (e->precision == VXG_FP32C) {
+    size_t vb = ((sizeof(float) * 16 * (size_t)nv + 255) / 256) * 256;
+    size_t lb = ((sizeof(float) * 22 * (size_t)nl + 255) / 256) * 256;
+    VXG_CK(cudaMalloc(&e->arena32, std::max<size_t>(vb + lb, 256)));
+    VXG_CK(cudaMemsetAsync(e->arena32, 0, vb + lb, e->stream));
+    float* p = (float*)e->arena32;
+    e->V.d = p; e->V.c = p + 3 * (size_t)nv; e->V.q = p + 6 * (size_t)nv;
+    e->V.lin = p + 10 * (size_t)nv; e->V.ang = p + 13 * (size_t)nv;
+    float* L = (float*)(e->arena32 + vb);
+    e->V.pos2 = L; e->V.a1v = L + 3 * (size_t)nl; e->V.a2v = L + 6 * (size_t)nl; e->V.fN = L + 9 * (size_t)nl;
+    e->V.fP = L + 12 * (size_t)nl; e->V.mN = L + 15 * (size_t)nl; e->V.mP = L + 18 * (size_t)nl;
+    e->V.restDelta = L + 21 * (size_t)nl;
+  }
   int rc = e->col.resize(nv);
   if (rc) return fail(e, rc, "collision buffers");
   VXG_CK(cudaMemsetAsync(e->ctl, 0, sizeof(Ctl), e->stream));
@@ -427,6 +567,10 @@ int vxg_set_field(vxg_engine* e, int f, const void* host, long long count) {
   long long n = (long long)d.comps * (d.per_link ? e->nl : e->nv);
   if (count != n) return fail(e, VXG_E_SIZE, "vxg_set_field: element count mismatch");
   if (n == 0) return VXG_OK;
+  if (e->precision == VXG_FP32C && is_state_field(f)) {
+    ensure64(e);  // keep the fields not overwritten here current before they are converted back
+    e->fp64_dirty = true;
+  }
   VXG_CK(cudaMemcpyAsync(e->field_ptr[f], host, (size_t)n * d.elem, cudaMemcpyHostToDevice, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
   return VXG_OK;
@@ -445,6 +589,7 @@ int vxg_get_field(vxg_engine* e, int f, void* host, long long count) {
   long long n = (long long)d.comps * (d.per_link ? e->nl : e->nv);
   if (count != n) return fail(e, VXG_E_SIZE, "vxg_get_field: element count mismatch");
   if (n == 0) return VXG_OK;
+  if (is_state_field(f)) ensure64(e);
   VXG_CK(cudaMemcpyAsync(host, e->field_ptr[f], (size_t)n * d.elem, cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
   return VXG_OK;
@@ -487,8 +632,10 @@ int vxg_set_powf_table(vxg_engine* e, int slot, float /*exponent*/, const float*
 
 int vxg_set_globals(vxg_engine* e, const vxg_globals* g) {
   if (!e || !g) return VXG_E_ARG;
+  if (e->precision == VXG_FP32C && g->collisions) return fail(e, VXG_E_ARG, "collisions run in FP64 precision only");
   e->g = *g;
   e->have_globals = true;
+  e->V.s = (float)g->voxSize;
   e->graph_valid = false;
   return VXG_OK;
 }
@@ -508,6 +655,18 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, cudaEvent_t* ev = 
   bool rec = dt < 0;
   if (ev) cudaEventRecord(ev[0], e->stream);
   if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S);
+  if (e->precision == VXG_FP32C) {
+    if (e->nl) {
+      if (rec) k_link32<true, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, parity);
+      else k_link32<false, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, parity);
+    }
+    if (ev) cudaEventRecord(ev[1], e->stream);
+    if (ev) cudaEventRecord(ev[2], e->stream);
+    if (rec) k_voxel32<true><<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+    else k_voxel32<false><<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+    if (ev) cudaEventRecord(ev[3], e->stream);
+    return;
+  }
   if (e->nl) {
     if (rec) k_link<true, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(S, parity);
     else k_link<false, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(S, parity);
@@ -530,6 +689,8 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
     return VXG_OK;
   }
   VXG_CK(cudaSetDevice(e->device));
+  ensure32(e);
+  if (e->precision == VXG_FP32C) e->fp32_ahead = true;
   // reset the per-batch control words (keep time and counters)
   int zeros[4] = {0, 0, 0, 0};
   VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
@@ -597,8 +758,14 @@ int vxg_recommended_dt(vxg_engine* e, float* dt) {
   VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
   unsigned z = 0u;
   VXG_CK(cudaMemcpyAsync(&e->ctl->maxf[0], &z, 4, cudaMemcpyHostToDevice, e->stream));
+  ensure32(e);
   if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S);
-  if (e->nl) k_link<true, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S, 0);
+  if (e->precision == VXG_FP32C) {
+    if (e->nl) k_link32<true, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, 0);
+    e->fp32_ahead = true;
+  } else if (e->nl) {
+    k_link<true, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S, 0);
+  }
   unsigned u = 0;
   VXG_CK(cudaMemcpyAsync(&u, &e->ctl->maxf[0], 4, cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
@@ -613,8 +780,14 @@ int vxg_recommended_dt(vxg_engine* e, float* dt) {
 int vxg_set_all_temperatures(vxg_engine* e, float t) {
   if (!e) return VXG_E_ARG;
   VXG_CK(cudaSetDevice(e->device));
+  ensure32(e);
   if (e->nv) k_set_temp<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S, t);
-  if (e->nl) k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
+  if (e->precision == VXG_FP32C) {
+    if (e->nl) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
+    e->fp32_ahead = true;
+  } else if (e->nl) {
+    k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
+  }
   VXG_CK(cudaGetLastError());
   return VXG_OK;
 }
@@ -622,8 +795,14 @@ int vxg_set_all_temperatures(vxg_engine* e, float t) {
 int vxg_set_temperatures(vxg_engine* e, const float* t) {
   if (!e || (!t && e->nv)) return VXG_E_ARG;
   VXG_CK(cudaSetDevice(e->device));
+  ensure32(e);
   if (e->nv) VXG_CK(cudaMemcpyAsync(e->S.temp, t, sizeof(float) * (size_t)e->nv, cudaMemcpyHostToDevice, e->stream));
-  if (e->nl) k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
+  if (e->precision == VXG_FP32C) {
+    if (e->nl) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
+    e->fp32_ahead = true;
+  } else if (e->nl) {
+    k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
+  }
   VXG_CK(cudaGetLastError());
   return VXG_OK;
 }
@@ -635,6 +814,7 @@ int vxg_reduce(vxg_engine* e, int info, int type, float* out) {
   int n = link ? e->nl : e->nv;
   if (n == 0) { *out = 0.0f; return VXG_OK; }
   if (info == 8) return fail(e, VXG_E_ARG, "PRESSURE is reduced on the host");
+  ensure64(e);
   int blocks = std::min(4096, grid_for(n));
   k_reduce<<<blocks, kBlock, 0, e->stream>>>(e->S, info, n, e->d_partials);
   std::vector<double> h((size_t)3 * blocks);

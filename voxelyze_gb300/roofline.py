@@ -33,3 +33,27 @@ def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
         link += FP64_POISSON_PER_VOXEL * n_voxels + FP64_POISSON_PER_LINK * n_links
     voxel = FP64_VOXEL_PER_VOXEL * n_voxels + FP64_VOXEL_PER_LINK * n_links
     return {"link": link, "voxel": voxel, "step": link + voxel}
+
+
+# FP32C layout (voxelyze_gb300/csrc/vx_phys32.cuh):
+#   link pass, per link : endpoint ids 8, flags 4+4, material id 4, previous pos2/angle1v/angle2v
+#                         36 read + 36 written, rest offset 4, transverse area/strain sum 8 read +
+#                         8 written, strain/maxStrain/strainOffset 12 read + 16 written, forces and
+#                         moments 48 written                                              = 188 B
+#             per voxel : displacement 12, orientation 16, material id 4                  =  32 B
+#   voxel pass, per voxel: displacement, compensation, orientation, momenta 64 read + 64 written,
+#                         flags 4+4, material id 4, external id 4, 6 link ids 24, lattice z 4,
+#                         temperature 4                                                  = 176 B
+#             per link  : the force and moment each end gathers, 2 x 24                   =  48 B
+FP32C_LINK_PER_LINK = 188
+FP32C_LINK_PER_VOXEL = 32
+FP32C_VOXEL_PER_VOXEL = 176
+FP32C_VOXEL_PER_LINK = 48
+
+
+def fp32c_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
+    link = FP32C_LINK_PER_LINK * n_links + FP32C_LINK_PER_VOXEL * n_voxels
+    if poisson:
+        link += FP64_POISSON_PER_VOXEL * n_voxels + FP64_POISSON_PER_LINK * n_links
+    voxel = FP32C_VOXEL_PER_VOXEL * n_voxels + FP32C_VOXEL_PER_LINK * n_links
+    return {"link": link, "voxel": voxel, "step": link + voxel}
