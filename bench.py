@@ -197,21 +197,7 @@ def run_ours(args, world, rank, local):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        import torch
-        import torch.distributed as dist
-
-        t = torch.tensor([x], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    from voxelyze_gb300.replicas import aggregate_rate, barrier
 
     lib = vg.library()
     lib.vx_step_timing.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
@@ -230,8 +216,8 @@ def run_ours(args, world, rank, local):
     t_head = _timed(lib, head, args.steps, dt, local, barrier)
     t_other = _timed(lib, other, args.steps, dt, local, barrier)
     for t in (t_head, t_other):
-        t["total_ms"] = max_over_ranks(t["total_ms"])
-        t["value"] = world * nv * args.steps / (t["total_ms"] / 1e3)
+        t["value"], _, secs = aggregate_rate(nv * args.steps, t["total_ms"] / 1e3)
+        t["total_ms"] = 1e3 * secs
 
     # FP32C error against the FP64 path (bit-identical to the FP64 oracle) after the same steps
     p64 = sim64.voxel_state()["pos"]
@@ -259,9 +245,8 @@ def run_ours(args, world, rank, local):
             raise RuntimeError("e2e step diverged")
         if lib.vx_read_positions(h, pos.data_ptr()) != 0:
             raise RuntimeError("vx_read_positions failed")
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value, _, _ = aggregate_rate(nv * e2e_steps, time.perf_counter() - t0)
     barrier()
-    e2e_value = world * nv * e2e_steps / e2e_s
 
     # ---- roofline of the dominant pass of the headline precision ------------------------------
     fp32 = head is sim32

@@ -49,7 +49,10 @@ enum { VXG_LF_SMALL_ANGLE = 1, VXG_LF_LOCAL_VEL_VALID = 2 };
 typedef struct {
   float E, nu, rho, alphaCTE, muStatic, muKinetic, zetaInternal, zetaGlobal, zetaCollision;
   float mass, massInv, sqrtMass, inertia, inertiaInv, c2xSqMxExS, c2xSqIxExSxSxS;
-  float gravMult, penetrationStiffness, eHat, pad0;
+  float gravMult, penetrationStiffness, eHat;
+  float nomSizeF;  /* FP32 copies for the FP32C path, which runs no FP64 arithmetic */
+  float sizeF[3];
+  float sizeAvgF;  /* (size.x + size.y + size.z) / 3 */
   double nomSize;
   double size[3];  /* nomSize * external scale factor per axis (CVX_MaterialVoxel::size) */
   int powf_slot;   /* powf table slot for exponent -nu, -1 when nu == 0 */

@@ -42,7 +42,7 @@ def test_lattice_1000_steps(product_lib):
     rel_pos, rel_disp = _errors(a, b, sc)
     print(f"lattice 128x128x64, 1000 steps: rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
     assert rel_pos <= 1e-5
-    assert rel_disp <= 1e-2
+    assert rel_disp <= 1e-3
 
 
 def test_small_lattice_poisson_dt_every_step(product_lib):
@@ -53,10 +53,19 @@ def test_small_lattice_poisson_dt_every_step(product_lib):
     rel_pos, rel_disp = _errors(a, b, sc)
     print(f"lattice 16x16x8, dt every step, 300 steps: rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
     assert rel_pos <= 1e-5
+    assert rel_disp <= 1e-3
 
 
-def test_population_with_temperature(product_lib):
+@pytest.mark.parametrize("friction", [False, True])
+def test_population_with_temperature(product_lib, friction):
+    """Bodies on the floor with CTE actuation.  Without friction FP32C tracks FP64 closely.  With
+    friction, the static-friction latch compares the horizontal force against mu * N while the
+    normal force N is still ~0 at first contact (VX_Voxel.cpp:285-291); FP32 rounding noise flips
+    that ill-conditioned test for some voxels, which then slide, so the bound is looser."""
     sc = S.population(16, 4, 10)
+    if not friction:
+        for m in sc.materials:
+            m.mu_static = m.mu_kinetic = 0.0
     a, b = _pair(product_lib, sc)
     dt = a.recommended_time_step()
     b.recommended_time_step()
@@ -67,8 +76,13 @@ def test_population_with_temperature(product_lib):
         assert a.do_time_steps(50, dt) == 50
         assert b.do_time_steps(50, dt) == 50
     rel_pos, rel_disp = _errors(a, b, sc)
-    print(f"population 16 bodies, CTE actuation, 500 steps: rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
-    assert rel_pos <= 1e-5
+    print(f"population 16 bodies, CTE actuation, friction={friction}, 500 steps: "
+          f"rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
+    if friction:
+        assert rel_pos <= 1e-3
+    else:
+        assert rel_pos <= 1e-6
+        assert rel_disp <= 1e-3
 
 
 def test_cantilever_small_deflection(product_lib):
@@ -82,7 +96,7 @@ def test_cantilever_small_deflection(product_lib):
     rel_pos, rel_disp = _errors(a, b, sc)
     print(f"cantilever 20x4x4, 3000 steps: rel pos err {rel_pos:.3e}, rel disp err {rel_disp:.3e}")
     assert rel_pos <= 1e-5
-    assert rel_disp <= 1e-3
+    assert rel_disp <= 2e-4
 
 
 def test_fp32c_state_roundtrip_and_reset(product_lib):

@@ -530,6 +530,9 @@ bool CVoxelyze::flush() {
       d.nomSize = m->nomSize;
       Vec3D<double> sz = m->size();
       d.size[0] = sz.x; d.size[1] = sz.y; d.size[2] = sz.z;
+      d.nomSizeF = (float)m->nomSize;
+      d.sizeF[0] = (float)sz.x; d.sizeF[1] = (float)sz.y; d.sizeF[2] = (float)sz.z;
+      d.sizeAvgF = (float)((sz.x + sz.y + sz.z) / 3.0);
       d.powf_slot = -1;
       if (m->nu != 0.0f) {
         any_poisson = true;

@@ -76,8 +76,9 @@ VX_HD q4 qmul(const q4& a, const q4& f) {
             a.w * f.y - a.x * f.z + a.y * f.w + a.z * f.x, a.w * f.z + a.x * f.y - a.y * f.x + a.z * f.w);
 }
 VX_HD f3 to_rotation_vector(const q4& q) {
-  if (q.w >= 1.0f || q.w <= -1.0f) return F3(0, 0, 0);
-  // 1 - w^2 from the vector part: no cancellation for w close to 1
+  // In FP32, w = cos(angle/2) rounds to exactly 1 for angles below ~5e-4 rad, so the FP64 test
+  // "w >= 1 means no rotation" would drop every small relative rotation; the vector part decides.
+  // |v| = sin(angle/2) comes from the vector part: no cancellation for w close to 1.
   float sl = q.x * q.x + q.y * q.y + q.z * q.z;
   if (sl <= 0.0f) return F3(0, 0, 0);
   float vl = sqrtf(sl);
@@ -132,9 +133,22 @@ VX_HD f3 to_axis_original(int axis, const f3& v) { return axis == 1 ? F3(-v.y, v
 VX_HD float rest_delta(const View& S, int vn, int vp, int axis) {
   const vxg_voxel_material& a = S.B.vm[S.B.vmat[vn]];
   const vxg_voxel_material& b = S.B.vm[S.B.vmat[vp]];
-  float ea = (float)a.size[axis] * (S.B.temp[vn] * a.alphaCTE) + ((float)a.size[axis] - S.s);
-  float eb = (float)b.size[axis] * (S.B.temp[vp] * b.alphaCTE) + ((float)b.size[axis] - S.s);
+  float ea = a.sizeF[axis] * (S.B.temp[vn] * a.alphaCTE) + (a.sizeF[axis] - S.s);
+  float eb = b.sizeF[axis] * (S.B.temp[vp] * b.alphaCTE) + (b.sizeF[axis] - S.s);
   return 0.5f * (ea + eb);
+}
+// CVX_Voxel::transverseArea in FP32 (the FP64 path's promotions would put double operations on
+// GB300's slow FP64 pipe for every link)
+VX_HD float transverse_area32(const vx64::View& B, int v, int axis) {
+  const vxg_voxel_material& m = B.vm[B.vmat[v]];
+  float size = m.nomSizeF;
+  if (m.nu == 0) return size * size;
+  float px = B.pStrain[v], py = B.pStrain[B.nv + v], pz = B.pStrain[2 * B.nv + v];
+  switch (axis) {
+    case 0: return size * size * (1 + py) * (1 + pz);
+    case 1: return size * size * (1 + px) * (1 + pz);
+    default: return size * size * (1 + px) * (1 + py);
+  }
 }
 
 VX_HD float link_freq2(const View& S, int l, int vn, int vp, int axis, const vxg_link_material& m) {
@@ -143,7 +157,7 @@ VX_HD float link_freq2(const View& S, int l, int vn, int vp, int axis, const vxg
     k = m.a1;
   } else {
     float rd = rest_delta(S, vn, vp, axis);
-    float ta = 0.5f * (vx64::transverse_area(S.B, vn, axis) + vx64::transverse_area(S.B, vp, axis));
+    float ta = 0.5f * (transverse_area32(S.B, vn, axis) + transverse_area32(S.B, vp, axis));
     float ts = 0.5f * (vx64::transverse_strain_sum(S.B, vn, axis) + vx64::transverse_strain_sum(S.B, vp, axis));
     S.restDelta[l] = rd;
     S.B.tArea[l] = ta;
@@ -212,7 +226,7 @@ VX_HDN void link_update(const View& S, int l) {
 
   float tArea = B.tArea[l], tSS = B.tSS[l];
   if (!(m.nu == 0.0f) || tSS != 0) {
-    tArea = 0.5f * (vx64::transverse_area(B, vn, axis) + vx64::transverse_area(B, vp, axis));
+    tArea = 0.5f * (transverse_area32(B, vn, axis) + transverse_area32(B, vp, axis));
     tSS = 0.5f * (vx64::transverse_strain_sum(B, vn, axis) + vx64::transverse_strain_sum(B, vp, axis));
     B.tArea[l] = tArea;
     B.tSS[l] = tSS;
@@ -330,7 +344,7 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   bool floorOn = flags & VXG_VF_FLOOR;
   bool staticF = flags & VXG_VF_STATIC_FRICTION;
   // floor penetration: (base size - nominal)/2 - z, with z = iz s + d.z
-  float expand = (float)((m.size[0] + m.size[1] + m.size[2]) / 3.0) * (1 + B.temp[v] * m.alphaCTE) - (float)m.nomSize;
+  float expand = m.sizeAvgF * (1 + B.temp[v] * m.alphaCTE) - m.nomSizeF;
   float zorg = (float)B.vidx[2 * nv + v] * S.s;
   float pen = (0.5f * expand - zorg) - (d.z - c.z);
   if (floorOn) {

@@ -226,60 +226,54 @@ __global__ void __launch_bounds__(kBlock) k_voxel32(vx32::View S, float dt_fixed
   if (v >= S.B.nv) return;
   vx32::voxel_update(S, v, dt);
 }
-// FP64 interchange fields -> FP32C working state (on upload) and back (on read)
-__global__ void k_to32(vx32::View S, double s) {
+// FP64 interchange fields <-> FP32C working state, one field per launch (only the fields the host
+// writes are converted on upload, only the fields it reads on download)
+__global__ void k_conv(vx32::View S, double s, int field, int to32) {
   const vx64::View& B = S.B;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < B.nv) {
-    for (int k = 0; k < 3; ++k) {
-      double dd = B.pos[k * B.nv + i] - B.vidx[k * B.nv + i] * s;
-      float d = (float)dd;
-      S.d[k * B.nv + i] = d;
-      S.c[k * B.nv + i] = (float)((double)d - dd);
-      S.lin[k * B.nv + i] = (float)B.linMom[k * B.nv + i];
-      S.ang[k * B.nv + i] = (float)B.angMom[k * B.nv + i];
+  const int nv = B.nv, nl = B.nl;
+  auto cv = [&](double* d64, float* d32, int comps, int n) {
+    if (i >= n) return;
+    for (int k = 0; k < comps; ++k) {
+      if (to32) d32[k * n + i] = (float)d64[k * n + i];
+      else d64[k * n + i] = d32[k * n + i];
     }
-    for (int k = 0; k < 4; ++k) S.q[k * B.nv + i] = (float)B.orient[k * B.nv + i];
-    if (i == 0) B.ctl->last_dt = B.prevDt[0];
-  }
-  if (i < B.nl) {
-    for (int k = 0; k < 3; ++k) {
-      int j = k * B.nl + i;
-      S.pos2[j] = (float)B.pos2[j];
-      S.a1v[j] = (float)B.a1v[j];
-      S.a2v[j] = (float)B.a2v[j];
-      S.fN[j] = (float)B.fN[j];
-      S.fP[j] = (float)B.fP[j];
-      S.mN[j] = (float)B.mN[j];
-      S.mP[j] = (float)B.mP[j];
-    }
-    S.restDelta[i] = (float)(B.rest[i] - s);
-  }
-}
-__global__ void k_to64(vx32::View S, double s) {
-  const vx64::View& B = S.B;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < B.nv) {
-    for (int k = 0; k < 3; ++k) {
-      B.pos[k * B.nv + i] = B.vidx[k * B.nv + i] * s + ((double)S.d[k * B.nv + i] - (double)S.c[k * B.nv + i]);
-      B.linMom[k * B.nv + i] = S.lin[k * B.nv + i];
-      B.angMom[k * B.nv + i] = S.ang[k * B.nv + i];
-    }
-    for (int k = 0; k < 4; ++k) B.orient[k * B.nv + i] = S.q[k * B.nv + i];
-    B.prevDt[i] = B.ctl->last_dt;
-  }
-  if (i < B.nl) {
-    for (int k = 0; k < 3; ++k) {
-      int j = k * B.nl + i;
-      B.pos2[j] = S.pos2[j];
-      B.a1v[j] = S.a1v[j];
-      B.a2v[j] = S.a2v[j];
-      B.fN[j] = S.fN[j];
-      B.fP[j] = S.fP[j];
-      B.mN[j] = S.mN[j];
-      B.mP[j] = S.mP[j];
-    }
-    B.rest[i] = s + (double)S.restDelta[i];
+  };
+  switch (field) {
+    case VXG_F_POS:
+      if (i < nv)
+        for (int k = 0; k < 3; ++k) {
+          if (to32) {
+            double dd = B.pos[k * nv + i] - B.vidx[k * nv + i] * s;
+            float d = (float)dd;
+            S.d[k * nv + i] = d;
+            S.c[k * nv + i] = (float)((double)d - dd);  // true displacement = d - c
+          } else {
+            B.pos[k * nv + i] = B.vidx[k * nv + i] * s + ((double)S.d[k * nv + i] - (double)S.c[k * nv + i]);
+          }
+        }
+      break;
+    case VXG_F_LINMOM: cv(B.linMom, S.lin, 3, nv); break;
+    case VXG_F_ORIENT: cv(B.orient, S.q, 4, nv); break;
+    case VXG_F_ANGMOM: cv(B.angMom, S.ang, 3, nv); break;
+    case VXG_F_PREV_DT:
+      if (to32) { if (i == 0 && nv) B.ctl->last_dt = B.prevDt[0]; }
+      else if (i < nv) B.prevDt[i] = B.ctl->last_dt;
+      break;
+    case VXG_F_POS2: cv(B.pos2, S.pos2, 3, nl); break;
+    case VXG_F_ANGLE1V: cv(B.a1v, S.a1v, 3, nl); break;
+    case VXG_F_ANGLE2V: cv(B.a2v, S.a2v, 3, nl); break;
+    case VXG_F_FORCE_NEG: cv(B.fN, S.fN, 3, nl); break;
+    case VXG_F_FORCE_POS: cv(B.fP, S.fP, 3, nl); break;
+    case VXG_F_MOMENT_NEG: cv(B.mN, S.mN, 3, nl); break;
+    case VXG_F_MOMENT_POS: cv(B.mP, S.mP, 3, nl); break;
+    case VXG_F_REST_LENGTH:
+      if (i < nl) {
+        if (to32) S.restDelta[i] = (float)(B.rest[i] - s);
+        else B.rest[i] = s + (double)S.restDelta[i];
+      }
+      break;
+    default: break;
   }
 }
 __global__ void k_rest32(vx32::View S) {
@@ -337,8 +331,8 @@ struct vxg_engine {
   View S{};
   vx32::View V{};          // FP32C working state (precision == VXG_FP32C)
   char* arena32 = nullptr;
-  bool fp64_dirty = false; // FP64 interchange fields written since the last conversion
-  bool fp32_ahead = false; // FP32C state newer than the FP64 interchange fields
+  uint32_t dirty64 = 0;    // FP32C: state fields the host wrote, not yet converted to FP32
+  uint32_t stale64 = 0;    // FP32C: state fields whose FP64 copy is older than the FP32 state
   Ctl* ctl = nullptr;
   vxg_voxel_material* d_vm = nullptr;
   vxg_link_material* d_lm = nullptr;
@@ -439,18 +433,30 @@ static bool is_state_field(int f) {
          f == VXG_F_POS2 || f == VXG_F_ANGLE1V || f == VXG_F_ANGLE2V || f == VXG_F_FORCE_NEG ||
          f == VXG_F_FORCE_POS || f == VXG_F_MOMENT_NEG || f == VXG_F_MOMENT_POS || f == VXG_F_REST_LENGTH;
 }
-// FP32C: bring the working state up to date with uploaded FP64 fields, or the reverse
-static void ensure32(vxg_engine* e) {
-  if (e->precision != VXG_FP32C || !e->fp64_dirty) return;
-  int n = std::max(e->nv, e->nl);
-  if (n) k_to32<<<grid_for(n), kBlock, 0, e->stream>>>(e->V, e->g.voxSize);
-  e->fp64_dirty = false;
+static uint32_t all_state_bits() {
+  uint32_t m = 0;
+  for (int f = 0; f < VXG_F_COUNT; ++f)
+    if (is_state_field(f)) m |= 1u << f;
+  return m;
 }
-static void ensure64(vxg_engine* e) {
-  if (e->precision != VXG_FP32C || !e->fp32_ahead) return;
+static void conv(vxg_engine* e, int f, int to32) {
   int n = std::max(e->nv, e->nl);
-  if (n) k_to64<<<grid_for(n), kBlock, 0, e->stream>>>(e->V, e->g.voxSize);
-  e->fp32_ahead = false;
+  if (n) k_conv<<<grid_for(n), kBlock, 0, e->stream>>>(e->V, e->g.voxSize, f, to32);
+}
+// FP32C: convert the fields the host wrote before the FP32 state is used
+static void ensure32(vxg_engine* e) {
+  if (e->precision != VXG_FP32C) return;
+  for (int f = 0; f < VXG_F_COUNT; ++f)
+    if (e->dirty64 & (1u << f)) conv(e, f, 1);
+  e->dirty64 = 0;
+}
+// FP32C: refresh the FP64 copy of one field (or all with f < 0) before it is read
+static void ensure64(vxg_engine* e, int f = -1) {
+  if (e->precision != VXG_FP32C) return;
+  uint32_t want = f < 0 ? e->stale64 : (e->stale64 & (1u << f));
+  for (int k = 0; k < VXG_F_COUNT; ++k)
+    if (want & (1u << k)) conv(e, k, 0);
+  e->stale64 &= ~want;
 }
 
 template <class T>
@@ -568,8 +574,8 @@ int vxg_set_field(vxg_engine* e, int f, const void* host, long long count) {
   if (count != n) return fail(e, VXG_E_SIZE, "vxg_set_field: element count mismatch");
   if (n == 0) return VXG_OK;
   if (e->precision == VXG_FP32C && is_state_field(f)) {
-    ensure64(e);  // keep the fields not overwritten here current before they are converted back
-    e->fp64_dirty = true;
+    e->dirty64 |= 1u << f;   // the FP64 copy is now the newer one
+    e->stale64 &= ~(1u << f);
   }
   VXG_CK(cudaMemcpyAsync(e->field_ptr[f], host, (size_t)n * d.elem, cudaMemcpyHostToDevice, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
@@ -589,7 +595,7 @@ int vxg_get_field(vxg_engine* e, int f, void* host, long long count) {
   long long n = (long long)d.comps * (d.per_link ? e->nl : e->nv);
   if (count != n) return fail(e, VXG_E_SIZE, "vxg_get_field: element count mismatch");
   if (n == 0) return VXG_OK;
-  if (is_state_field(f)) ensure64(e);
+  if (is_state_field(f)) ensure64(e, f);
   VXG_CK(cudaMemcpyAsync(host, e->field_ptr[f], (size_t)n * d.elem, cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
   return VXG_OK;
@@ -690,7 +696,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   }
   VXG_CK(cudaSetDevice(e->device));
   ensure32(e);
-  if (e->precision == VXG_FP32C) e->fp32_ahead = true;
+  if (e->precision == VXG_FP32C) e->stale64 = all_state_bits();
   // reset the per-batch control words (keep time and counters)
   int zeros[4] = {0, 0, 0, 0};
   VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
@@ -762,7 +768,7 @@ int vxg_recommended_dt(vxg_engine* e, float* dt) {
   if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S);
   if (e->precision == VXG_FP32C) {
     if (e->nl) k_link32<true, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, 0);
-    e->fp32_ahead = true;
+    e->stale64 |= 1u << VXG_F_REST_LENGTH;
   } else if (e->nl) {
     k_link<true, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S, 0);
   }
@@ -784,7 +790,7 @@ int vxg_set_all_temperatures(vxg_engine* e, float t) {
   if (e->nv) k_set_temp<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S, t);
   if (e->precision == VXG_FP32C) {
     if (e->nl) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
-    e->fp32_ahead = true;
+    e->stale64 |= 1u << VXG_F_REST_LENGTH;
   } else if (e->nl) {
     k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
   }
@@ -799,7 +805,7 @@ int vxg_set_temperatures(vxg_engine* e, const float* t) {
   if (e->nv) VXG_CK(cudaMemcpyAsync(e->S.temp, t, sizeof(float) * (size_t)e->nv, cudaMemcpyHostToDevice, e->stream));
   if (e->precision == VXG_FP32C) {
     if (e->nl) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
-    e->fp32_ahead = true;
+    e->stale64 |= 1u << VXG_F_REST_LENGTH;
   } else if (e->nl) {
     k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
   }
