@@ -56,6 +56,14 @@ int vx_counters(void* s, long long* out, int n);            /* vxg_counters of t
 int vx_enable_timing(void* s, int on);                      /* vxg_enable_timing */
 int vx_step_timing(void* s, float* out4);                   /* batch ms, link/collide/voxel ms per step */
 const char* vx_last_error(void* s);
+/* per-step temperature actuation inside the GPU step, see vxg_set_actuation (mode 0 off, 1 one
+ * phase, 2 per-voxel phase[n_voxels]); kept across topology edits */
+int vx_set_actuation(void* s, int mode, double amplitude, double frequency, const float* phase);
+int vx_body_com(void* s, const int* offsets, int n_bodies, double* out);   /* vxg_body_com */
+int vx_snapshot(void* s, int slot);                         /* vxg_snapshot: device checkpoint */
+int vx_restore(void* s, int slot);                          /* vxg_restore (same scene only) */
+int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk); /* vxg_set_launch */
+int vx_autotune(void* s, int trial_steps, float dt, int* out3);            /* vxg_autotune: link, voxel, chunk */
 
 #ifdef __cplusplus
 }

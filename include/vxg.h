@@ -169,6 +169,25 @@ int vxg_reduce(vxg_engine* e, int info, int type, float* out);
  * Returns the pair count through *n (pairs beyond cap are not written). */
 int vxg_get_collisions(vxg_engine* e, int* pairs, int cap, int* n);
 int vxg_counters(vxg_engine* e, long long* out, int n);
+/* Per-step actuation inside the step (and inside captured graphs): before every step's link pass
+ * each voxel's temperature becomes amplitude * sin(2 pi frequency t + phase) with t the current
+ * time, and every rest length follows - the reference's setAmbientTemperature(T, true) (mode 1)
+ * or per-voxel setTemperature (mode 2, phase[n_voxels]) called before each doTimeStep
+ * (src/Voxelyze.cpp:585-594, src/VX_Voxel.cpp:108-114).  Mode 0 turns it off. */
+int vxg_set_actuation(vxg_engine* e, int mode, double amplitude, double frequency, const float* phase);
+/* Mass-weighted centre of mass of each body, bodies being contiguous voxel ranges
+ * [offsets[b], offsets[b+1]); out receives 3 doubles per body. */
+int vxg_body_com(vxg_engine* e, const int* offsets, int n_bodies, double* out);
+/* Launch shapes: threads per block of the link and voxel passes (64..512, 0 keeps the current) and
+ * the number of steps per captured CUDA graph replayed for long runs (even; 0 keeps). */
+int vxg_set_launch(vxg_engine* e, int block_link, int block_voxel, int graph_chunk);
+int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_chunk);
+/* Times short runs of the current scene for every block-size pair and several graph lengths and
+ * keeps the fastest; the state is restored afterwards. */
+int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* best_voxel, int* best_chunk);
+/* Full device-side copies of the simulation state (checkpoint / restart). */
+int vxg_snapshot(vxg_engine* e, int slot);
+int vxg_restore(vxg_engine* e, int slot);
 /* Timing mode: vxg_step records CUDA events on the engine stream around the link pass (with the
  * Poisson pre-pass), the collision stage and the voxel pass of every step (no graph replay).
  * vxg_last_step_timing gives the per-step averages of the last batch in milliseconds,

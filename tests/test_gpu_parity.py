@@ -191,3 +191,25 @@ def test_large_lattice_full_size(product_lib, cr_oracle, dims):
     pos = g.voxel_state()["pos"]
     assert np.all(np.isfinite(pos))
     assert pos[:, 2].min() > -0.5 * sc.voxel_size
+
+
+def test_state_info_device_reduction(product_lib, cr_oracle):
+    """vxg_reduce (CVoxelyze::stateInfoDevice): MIN and MAX equal the reference's serial float
+    reduction exactly; TOTAL and AVERAGE accumulate in double, within 1e-5 of it."""
+    sc = S.lattice(20, 16, 10)
+    g, o = _pair(product_lib, cr_oracle, sc)
+    dt = o.recommended_time_step()
+    g.do_time_steps(120, dt)
+    o.do_time_steps(120, dt)
+    f = product_lib.vx_state_info_device
+    f.restype = C.c_float
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    for info in (F.DISPLACEMENT, F.VELOCITY, F.KINETIC_ENERGY, F.ANGULAR_VELOCITY, F.ENG_STRESS, F.ENG_STRAIN,
+                 F.STRAIN_ENERGY, F.MASS):
+        for t in (F.MIN, F.MAX, F.TOTAL, F.AVERAGE):
+            dev = f(C.c_void_p(g.h), info, t)
+            ref = o.state_info(info, t)
+            if t in (F.MIN, F.MAX):
+                assert dev == ref, (info, t, dev, ref)
+            else:
+                assert abs(dev - ref) <= 1e-5 * max(abs(ref), 1e-30), (info, t, dev, ref)

@@ -477,6 +477,7 @@ bool CVoxelyze::flush() {
     I.topo_dirty = I.tables_dirty = I.state_dirty = I.nearby_dirty = true;
     I.powf_slots.clear();
   }
+  if (I.topo_dirty && I.act_mode) I.act_dirty = true;
   const int nv = (int)voxelsList.size(), nl = (int)linksList.size();
   std::unordered_map<const CVX_MaterialVoxel*, int> vmi;
   for (size_t k = 0; k < voxelMats.size(); ++k) vmi[voxelMats[k]] = (int)k;
@@ -633,6 +634,14 @@ bool CVoxelyze::flush() {
     }
     if (vxg_set_nearby(I.eng, off.data(), items.data(), (long long)items.size())) { I.err = vxg_last_error(I.eng); return false; }
     I.nearby_dirty = false;
+  }
+  if (I.act_dirty) {
+    if (I.act_mode == 2 && I.act_phase.size() != (size_t)nv) { I.err = "actuation phases do not match the voxel count"; return false; }
+    if (vxg_set_actuation(I.eng, I.act_mode, I.act_amp, I.act_freq, I.act_mode == 2 ? I.act_phase.data() : nullptr)) {
+      I.err = vxg_last_error(I.eng);
+      return false;
+    }
+    I.act_dirty = false;
   }
   return true;
 }
@@ -1320,5 +1329,52 @@ int vx_step_timing(void* s, float* out4) {
   return vxg_last_step_timing(e, &out4[1], &out4[2], &out4[3]);
 }
 const char* vx_last_error(void* s) { return H(s)->vx.lastError(); }
+int vx_set_actuation(void* s, int mode, double amplitude, double frequency, const float* phase) {
+  CVoxelyze& vx = H(s)->vx;
+  VxImpl& I = *vx.impl();
+  if (mode < 0 || mode > 2 || (mode == 2 && !phase && vx.voxelCount())) return -1;
+  vx.upload();
+  I.act_mode = mode;
+  I.act_amp = amplitude;
+  I.act_freq = frequency;
+  if (mode == 2) I.act_phase.assign(phase, phase + vx.voxelCount());
+  else I.act_phase.clear();
+  I.act_dirty = true;
+  return vx.upload() ? 0 : -1;
+}
+int vx_body_com(void* s, const int* offsets, int n_bodies, double* out) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  int rc = vxg_body_com(vx.impl()->eng, offsets, n_bodies, out);
+  if (rc) vx.impl()->err = vxg_last_error(vx.impl()->eng);
+  return rc ? -1 : 0;
+}
+int vx_snapshot(void* s, int slot) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  int rc = vxg_snapshot(vx.impl()->eng, slot);
+  if (rc) vx.impl()->err = vxg_last_error(vx.impl()->eng);
+  return rc ? -1 : 0;
+}
+int vx_restore(void* s, int slot) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  int rc = vxg_restore(vx.impl()->eng, slot);
+  if (rc) { vx.impl()->err = vxg_last_error(vx.impl()->eng); return -1; }
+  vx.impl()->device_ahead = true;
+  return 0;
+}
+int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_set_launch(vx.impl()->eng, block_link, block_voxel, graph_chunk) ? -1 : 0;
+}
+int vx_autotune(void* s, int trial_steps, float dt, int* out3) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload() || !out3) return -1;
+  int rc = vxg_autotune(vx.impl()->eng, trial_steps, dt, &out3[0], &out3[1], &out3[2]);
+  if (rc) vx.impl()->err = vxg_last_error(vx.impl()->eng);
+  return rc ? -1 : 0;
+}
 
 }  // extern "C"

@@ -44,6 +44,11 @@ struct VxImpl {
   bool state_dirty = true;   // host mirror edited
   bool device_ahead = false; // device state newer than the mirror
   bool nearby_dirty = true;  // collision lattice lists need regeneration
+  // per-step actuation handed to the engine (vxg_set_actuation); re-sent after topology changes
+  int act_mode = 0;
+  double act_amp = 0, act_freq = 0;
+  std::vector<float> act_phase;
+  bool act_dirty = false;
   std::map<float, int> powf_slots;  // exponent -> table slot already on the device
   std::string err;
 

@@ -330,6 +330,7 @@ struct Collide {
   ColView C{};
   ColCtl* cc = nullptr;
   char* buf = nullptr;
+  size_t buf_bytes = 0;
   int* d_nb = nullptr;  // nearby CSR storage (offsets then items)
   int nv = 0;
   int pcap = 0, wcap = 0;
@@ -376,6 +377,7 @@ struct Collide {
            o_pd = take(4 * (size_t)pcap), o_pf = take(12 * (size_t)pcap);
     if (n == 0) return VXG_OK;
     if (cudaMalloc(&buf, bytes) != cudaSuccess) return VXG_E_CUDA;
+    buf_bytes = bytes;
     if (cudaMemset(buf, 0, bytes) != cudaSuccess) return VXG_E_CUDA;
     C.nv = n;
     C.hcap_mask = hcap - 1;

@@ -62,7 +62,7 @@ __device__ __forceinline__ void block_max_to(unsigned* dst, float f) {
 }
 
 template <bool RECOMMEND, bool FORCES>
-__global__ void __launch_bounds__(kBlock) k_link(View S, int parity) {
+__global__ void __launch_bounds__(512) k_link(View S, int parity) {
   int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (S.ctl->halt) return;
   float f2 = 0.0f;
@@ -89,7 +89,7 @@ __device__ __forceinline__ float step_dt(const View& S, bool recommend, float dt
 }
 
 template <bool RECOMMEND>
-__global__ void __launch_bounds__(kBlock) k_voxel(View S, float dt_fixed, int parity, float fallback) {
+__global__ void __launch_bounds__(512) k_voxel(View S, float dt_fixed, int parity, float fallback) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (S.ctl->halt) return;
   if (S.ctl->diverged) {
@@ -189,10 +189,11 @@ __global__ void k_reduce(View S, int info, int n, double* out /* 3 per block: mi
 }
 
 int grid_for(int n) { return std::max(1, (n + kBlock - 1) / kBlock); }
+int grid_of(int n, int b) { return std::max(1, (n + b - 1) / b); }
 
 // ---- FP32C kernels ------------------------------------------------------------------------
 template <bool RECOMMEND, bool FORCES>
-__global__ void __launch_bounds__(kBlock) k_link32(vx32::View S, int parity) {
+__global__ void __launch_bounds__(512) k_link32(vx32::View S, int parity) {
   int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (S.B.ctl->halt) return;
   float f2 = 0.0f;
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(kBlock) k_link32(vx32::View S, int parity) {
 }
 
 template <bool RECOMMEND>
-__global__ void __launch_bounds__(kBlock) k_voxel32(vx32::View S, float dt_fixed, int parity, float fallback) {
+__global__ void __launch_bounds__(512) k_voxel32(vx32::View S, float dt_fixed, int parity, float fallback) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (S.B.ctl->halt) return;
   if (S.B.ctl->diverged) {
@@ -276,6 +277,61 @@ __global__ void k_conv(vx32::View S, double s, int field, int to32) {
     default: break;
   }
 }
+// Per-step actuation: before each step's link pass every voxel's temperature is set to
+//   amplitude * sin(2 pi frequency t + phase)      (t = CVoxelyze::currentTime at the step start)
+// and every rest length follows, i.e. the reference's setAmbientTemperature(T, true) (mode 1, one
+// phase) or CVX_Voxel::setTemperature per voxel (mode 2, per-voxel phase) before doTimeStep
+// (src/Voxelyze.cpp:585-594, src/VX_Voxel.cpp:108-114).  Evaluated in double with the correctly
+// rounded sine on the FP64 path, in float on the FP32C path; the result is rounded to float like
+// the reference's float temperature argument.
+__global__ void k_actuate(View S, double amp, double freq, const float* phase, int fp32) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= S.nv || S.ctl->halt) return;
+  double arg = 2.0 * 3.141592653589793 * freq * (double)S.ctl->time + (phase ? (double)phase[v] : 0.0);
+  float t;
+  if (fp32) {
+    t = (float)amp * sinf((float)arg);
+  } else {
+    int f = 0;
+    t = (float)(amp * vxm::cr_sin(arg, &f));
+  }
+  S.temp[v] = t;
+}
+
+// mass-weighted centre of mass of contiguous voxel ranges (one block per body), double accumulation
+__global__ void k_body_com(View S, const float* d32, const float* c32, double s, const int* off, double* out) {
+  int b = blockIdx.x;
+  int lo = off[b], hi = off[b + 1];
+  double m = 0, x = 0, y = 0, z = 0;
+  for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
+    double mv = S.vm[S.vmat[v]].mass, px, py, pz;
+    if (d32) {
+      px = S.vidx[v] * s + ((double)d32[v] - (double)c32[v]);
+      py = S.vidx[S.nv + v] * s + ((double)d32[S.nv + v] - (double)c32[S.nv + v]);
+      pz = S.vidx[2 * S.nv + v] * s + ((double)d32[2 * S.nv + v] - (double)c32[2 * S.nv + v]);
+    } else {
+      px = S.pos[v]; py = S.pos[S.nv + v]; pz = S.pos[2 * S.nv + v];
+    }
+    m += mv; x += mv * px; y += mv * py; z += mv * pz;
+  }
+  __shared__ double sh[4][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    m += __shfl_xor_sync(0xffffffffu, m, o);
+    x += __shfl_xor_sync(0xffffffffu, x, o);
+    y += __shfl_xor_sync(0xffffffffu, y, o);
+    z += __shfl_xor_sync(0xffffffffu, z, o);
+  }
+  int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if ((threadIdx.x & 31) == 0) { sh[0][w] = m; sh[1][w] = x; sh[2][w] = y; sh[3][w] = z; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < nw; ++k) { m += sh[0][k]; x += sh[1][k]; y += sh[2][k]; z += sh[3][k]; }
+    out[3 * b] = m > 0 ? x / m : 0.0;
+    out[3 * b + 1] = m > 0 ? y / m : 0.0;
+    out[3 * b + 2] = m > 0 ? z / m : 0.0;
+  }
+}
+
 __global__ void k_rest32(vx32::View S) {
   int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= S.B.nl) return;
@@ -331,6 +387,7 @@ struct vxg_engine {
   View S{};
   vx32::View V{};          // FP32C working state (precision == VXG_FP32C)
   char* arena32 = nullptr;
+  size_t arena32_bytes = 0;
   uint32_t dirty64 = 0;    // FP32C: state fields the host wrote, not yet converted to FP32
   uint32_t stale64 = 0;    // FP32C: state fields whose FP64 copy is older than the FP32 state
   Ctl* ctl = nullptr;
@@ -350,11 +407,33 @@ struct vxg_engine {
   int tev_used = 0;
   float t_link = 0, t_col = 0, t_vox = 0, t_batch = 0;
   std::string err;
-  // captured batches
+  // captured batches: a graph of `graph_chunk` steps replayed for long runs, and one for short ones
   cudaGraphExec_t graph = nullptr;
   int graph_n = -1;
   float graph_dt = 0;
   bool graph_valid = false;
+  cudaGraphExec_t cgraph = nullptr;
+  float cgraph_dt = 0;
+  int cgraph_n = -1;
+  int graph_chunk = 64;
+  // launch shapes (vxg_set_launch / vxg_autotune)
+  int blk_link = 256, blk_voxel = 256;
+  // per-step actuation (vxg_set_actuation)
+  int act_mode = 0;
+  double act_amp = 0, act_freq = 0;
+  float* d_phase = nullptr;
+  int n_phase = 0;
+  // scratch of the body centre-of-mass reduction
+  int* d_body_off = nullptr;
+  double* d_body_out = nullptr;
+  int n_body_cap = 0;
+  // device snapshots of the full state
+  struct Snap {
+    char* p[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t n[4] = {0, 0, 0, 0};
+    int nv = -1, nl = -1, precision = -1;
+  };
+  std::vector<Snap> snaps;
 };
 
 static int fail(vxg_engine* e, int code, const char* what, cudaError_t ce = cudaSuccess) {
@@ -501,6 +580,12 @@ int vxg_destroy(vxg_engine* e) {
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
   if (e->graph) cudaGraphExecDestroy(e->graph);
+  if (e->cgraph) cudaGraphExecDestroy(e->cgraph);
+  if (e->d_phase) cudaFree(e->d_phase);
+  if (e->d_body_off) cudaFree(e->d_body_off);
+  if (e->d_body_out) cudaFree(e->d_body_out);
+  for (auto& sl : e->snaps)
+    for (char* p : sl.p) if (p) cudaFree(p);
   release_arena(e);
   e->col.release();
   if (e->ctl) cudaFree(e->ctl);
@@ -542,7 +627,8 @@ int vxg_resize(vxg_engine* e, int nv, int nl) {
   if (e->precision == VXG_FP32C) {
     size_t vb = ((sizeof(float) * 16 * (size_t)nv + 255) / 256) * 256;
     size_t lb = ((sizeof(float) * 22 * (size_t)nl + 255) / 256) * 256;
-    VXG_CK(cudaMalloc(&e->arena32, std::max<size_t>(vb + lb, 256)));
+    e->arena32_bytes = std::max<size_t>(vb + lb, 256);
+    VXG_CK(cudaMalloc(&e->arena32, e->arena32_bytes));
     VXG_CK(cudaMemsetAsync(e->arena32, 0, vb + lb, e->stream));
     float* p = (float*)e->arena32;
     e->V.d = p; e->V.c = p + 3 * (size_t)nv; e->V.q = p + 6 * (size_t)nv;
@@ -659,30 +745,52 @@ int vxg_set_nearby(vxg_engine* e, const int* offsets, const int* items, long lon
 static void enqueue_step(vxg_engine* e, float dt, int parity, cudaEvent_t* ev = nullptr) {
   const View& S = e->S;
   bool rec = dt < 0;
+  const int bl = e->blk_link, bv = e->blk_voxel;
+  const int gl = grid_of(e->nl, bl), gv = grid_of(e->nv, bv);
   if (ev) cudaEventRecord(ev[0], e->stream);
+  if (e->act_mode && e->nv) {
+    k_actuate<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S, e->act_amp, e->act_freq, e->act_mode == 2 ? e->d_phase : nullptr,
+                                                        e->precision == VXG_FP32C ? 1 : 0);
+    if (e->nl) {
+      if (e->precision == VXG_FP32C) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
+      else k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(S);
+    }
+  }
   if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S);
   if (e->precision == VXG_FP32C) {
     if (e->nl) {
-      if (rec) k_link32<true, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, parity);
-      else k_link32<false, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, parity);
+      if (rec) k_link32<true, true><<<gl, bl, 0, e->stream>>>(e->V, parity);
+      else k_link32<false, true><<<gl, bl, 0, e->stream>>>(e->V, parity);
     }
     if (ev) cudaEventRecord(ev[1], e->stream);
     if (ev) cudaEventRecord(ev[2], e->stream);
-    if (rec) k_voxel32<true><<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
-    else k_voxel32<false><<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+    if (rec) k_voxel32<true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+    else k_voxel32<false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
     if (ev) cudaEventRecord(ev[3], e->stream);
     return;
   }
   if (e->nl) {
-    if (rec) k_link<true, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(S, parity);
-    else k_link<false, true><<<grid_for(e->nl), kBlock, 0, e->stream>>>(S, parity);
+    if (rec) k_link<true, true><<<gl, bl, 0, e->stream>>>(S, parity);
+    else k_link<false, true><<<gl, bl, 0, e->stream>>>(S, parity);
   }
   if (ev) cudaEventRecord(ev[1], e->stream);
   if (e->g.collisions) e->col.enqueue(e->g, e->stream);
   if (ev) cudaEventRecord(ev[2], e->stream);
-  if (rec) k_voxel<true><<<grid_for(e->nv), kBlock, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
-  else k_voxel<false><<<grid_for(e->nv), kBlock, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+  if (rec) k_voxel<true><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+  else k_voxel<false><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
   if (ev) cudaEventRecord(ev[3], e->stream);
+}
+
+static int capture(vxg_engine* e, int n, float dt, cudaGraphExec_t* out) {
+  if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
+  cudaGraph_t g;
+  VXG_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < n; ++s) enqueue_step(e, dt, s & 1);
+  VXG_CK(cudaStreamEndCapture(e->stream, &g));
+  cudaError_t c = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (c != cudaSuccess) return fail(e, VXG_E_CUDA, "graph instantiate", c);
+  return VXG_OK;
 }
 
 int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged) {
@@ -694,6 +802,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
     if (steps_done) *steps_done = nsteps;
     return VXG_OK;
   }
+  if (e->act_mode == 2 && e->n_phase < e->nv) return fail(e, VXG_E_STATE, "actuation phases cover fewer voxels than the scene");
   VXG_CK(cudaSetDevice(e->device));
   ensure32(e);
   if (e->precision == VXG_FP32C) e->stale64 = all_state_bits();
@@ -705,20 +814,32 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   bool use_graph = !e->timing && nsteps > 1;
   e->tev_used = 0;
   if (use_graph) {
-    if (!e->graph_valid || e->graph_n != nsteps || e->graph_dt != dt) {
-      if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
-      cudaGraph_t g;
-      VXG_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-      for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1);
-      VXG_CK(cudaStreamEndCapture(e->stream, &g));
-      cudaError_t c = cudaGraphInstantiate(&e->graph, g, 0);
-      cudaGraphDestroy(g);
-      if (c != cudaSuccess) return fail(e, VXG_E_CUDA, "graph instantiate", c);
-      e->graph_n = nsteps;
-      e->graph_dt = dt;
-      e->graph_valid = true;
+    int chunk = e->graph_chunk;
+    if (nsteps >= chunk) {
+      // long runs: one captured chunk (even length keeps the step parities aligned) replayed
+      if (!e->graph_valid || !e->cgraph || e->cgraph_dt != dt || e->cgraph_n != chunk) {
+        int rc = capture(e, chunk, dt, &e->cgraph);
+        if (rc) return rc;
+        e->cgraph_dt = dt;
+        e->cgraph_n = chunk;
+        if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+        e->graph_n = -1;
+        e->graph_valid = true;
+      }
+      int full = nsteps / chunk;
+      for (int k = 0; k < full; ++k) VXG_CK(cudaGraphLaunch(e->cgraph, e->stream));
+      for (int s = full * chunk; s < nsteps; ++s) enqueue_step(e, dt, s & 1);
+    } else {
+      if (!e->graph_valid || !e->graph || e->graph_n != nsteps || e->graph_dt != dt) {
+        int rc = capture(e, nsteps, dt, &e->graph);
+        if (rc) return rc;
+        e->graph_n = nsteps;
+        e->graph_dt = dt;
+        if (!e->graph_valid && e->cgraph) { cudaGraphExecDestroy(e->cgraph); e->cgraph = nullptr; }
+        e->graph_valid = true;
+      }
+      VXG_CK(cudaGraphLaunch(e->graph, e->stream));
     }
-    VXG_CK(cudaGraphLaunch(e->graph, e->stream));
   } else if (e->timing) {
     size_t need = (size_t)4 * nsteps;
     while (e->tev.size() < need) {
@@ -839,6 +960,175 @@ int vxg_reduce(vxg_engine* e, int info, int type, float* out) {
     default: *out = (float)(sm / n); break;
   }
   return VXG_OK;
+}
+
+int vxg_set_actuation(vxg_engine* e, int mode, double amplitude, double frequency, const float* phase) {
+  if (!e || mode < 0 || mode > 2 || (mode == 2 && !phase && e->nv)) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  if (mode == 2 && e->nv) {
+    if (e->n_phase < e->nv) {
+      if (e->d_phase) cudaFree(e->d_phase);
+      e->d_phase = nullptr;
+      VXG_CK(cudaMalloc(&e->d_phase, sizeof(float) * (size_t)e->nv));
+      e->n_phase = e->nv;
+    }
+    VXG_CK(cudaMemcpyAsync(e->d_phase, phase, sizeof(float) * (size_t)e->nv, cudaMemcpyHostToDevice, e->stream));
+    VXG_CK(cudaStreamSynchronize(e->stream));
+  }
+  e->act_mode = mode;
+  e->act_amp = amplitude;
+  e->act_freq = frequency;
+  e->graph_valid = false;
+  return VXG_OK;
+}
+
+int vxg_body_com(vxg_engine* e, const int* offsets, int n_bodies, double* out) {
+  if (!e || !offsets || !out || n_bodies <= 0) return VXG_E_ARG;
+  if (offsets[0] < 0 || offsets[n_bodies] > e->nv) return fail(e, VXG_E_SIZE, "vxg_body_com: offsets out of range");
+  VXG_CK(cudaSetDevice(e->device));
+  if (n_bodies > e->n_body_cap) {
+    if (e->d_body_off) cudaFree(e->d_body_off);
+    if (e->d_body_out) cudaFree(e->d_body_out);
+    e->d_body_off = nullptr;
+    e->d_body_out = nullptr;
+    VXG_CK(cudaMalloc(&e->d_body_off, sizeof(int) * ((size_t)n_bodies + 1)));
+    VXG_CK(cudaMalloc(&e->d_body_out, sizeof(double) * 3 * (size_t)n_bodies));
+    e->n_body_cap = n_bodies;
+  }
+  ensure32(e);
+  VXG_CK(cudaMemcpyAsync(e->d_body_off, offsets, sizeof(int) * ((size_t)n_bodies + 1), cudaMemcpyHostToDevice, e->stream));
+  bool fp32 = e->precision == VXG_FP32C;
+  k_body_com<<<n_bodies, 128, 0, e->stream>>>(e->S, fp32 ? e->V.d : nullptr, fp32 ? e->V.c : nullptr, e->g.voxSize,
+                                             e->d_body_off, e->d_body_out);
+  VXG_CK(cudaMemcpyAsync(out, e->d_body_out, sizeof(double) * 3 * (size_t)n_bodies, cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  VXG_CK(cudaGetLastError());
+  return VXG_OK;
+}
+
+int vxg_set_launch(vxg_engine* e, int block_link, int block_voxel, int graph_chunk) {
+  if (!e) return VXG_E_ARG;
+  auto ok = [](int b) { return b == 64 || b == 128 || b == 256 || b == 512; };
+  if ((block_link && !ok(block_link)) || (block_voxel && !ok(block_voxel)) || graph_chunk < 0) return VXG_E_ARG;
+  if (block_link) e->blk_link = block_link;
+  if (block_voxel) e->blk_voxel = block_voxel;
+  if (graph_chunk) e->graph_chunk = (graph_chunk + 1) & ~1;  // even: the step parity repeats
+  e->graph_valid = false;
+  return VXG_OK;
+}
+
+int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_chunk) {
+  if (!e) return VXG_E_ARG;
+  if (block_link) *block_link = e->blk_link;
+  if (block_voxel) *block_voxel = e->blk_voxel;
+  if (graph_chunk) *graph_chunk = e->graph_chunk;
+  return VXG_OK;
+}
+
+// Device copies of the whole simulation state (every field, the FP32C state, the control block
+// and the collision buffers) kept in device memory: checkpoints for restarts and recomputation.
+int vxg_snapshot(vxg_engine* e, int slot) {
+  if (!e || slot < 0 || slot > 1023) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  ensure32(e);
+  if ((int)e->snaps.size() <= slot) e->snaps.resize(slot + 1);
+  vxg_engine::Snap& sl = e->snaps[slot];
+  const size_t sizes[4] = {e->arena_bytes, e->arena32_bytes, sizeof(Ctl), e->col.buf_bytes};
+  char* const src[4] = {e->arena, e->arena32, (char*)e->ctl, e->col.buf};
+  for (int k = 0; k < 4; ++k) {
+    if (sl.p[k] && sl.n[k] != sizes[k]) { cudaFree(sl.p[k]); sl.p[k] = nullptr; sl.n[k] = 0; }
+    if (!src[k] || !sizes[k]) continue;
+    if (!sl.p[k]) VXG_CK(cudaMalloc(&sl.p[k], sizes[k]));
+    sl.n[k] = sizes[k];
+    VXG_CK(cudaMemcpyAsync(sl.p[k], src[k], sizes[k], cudaMemcpyDeviceToDevice, e->stream));
+  }
+  sl.nv = e->nv;
+  sl.nl = e->nl;
+  sl.precision = e->precision;
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  return VXG_OK;
+}
+
+int vxg_restore(vxg_engine* e, int slot) {
+  if (!e || slot < 0 || slot >= (int)e->snaps.size() || e->snaps[slot].nv < 0) return VXG_E_ARG;
+  vxg_engine::Snap& sl = e->snaps[slot];
+  const size_t sizes[4] = {e->arena_bytes, e->arena32_bytes, sizeof(Ctl), e->col.buf_bytes};
+  char* const dst[4] = {e->arena, e->arena32, (char*)e->ctl, e->col.buf};
+  if (sl.nv != e->nv || sl.nl != e->nl || sl.precision != e->precision)
+    return fail(e, VXG_E_STATE, "vxg_restore: the scene changed since the snapshot");
+  for (int k = 0; k < 4; ++k)
+    if ((sl.p[k] != nullptr) != (dst[k] != nullptr && sizes[k] != 0) || (sl.p[k] && sl.n[k] != sizes[k]))
+      return fail(e, VXG_E_STATE, "vxg_restore: buffer layout changed since the snapshot");
+  VXG_CK(cudaSetDevice(e->device));
+  for (int k = 0; k < 4; ++k)
+    if (sl.p[k]) VXG_CK(cudaMemcpyAsync(dst[k], sl.p[k], sizes[k], cudaMemcpyDeviceToDevice, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  if (e->precision == VXG_FP32C) {
+    e->dirty64 = 0;
+    e->stale64 = all_state_bits();
+  }
+  return VXG_OK;
+}
+
+// Picks the link and voxel block sizes and the graph chunk length by timing short runs on the
+// current scene; the state is snapshotted before and restored after, so the simulation is unchanged.
+int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* best_voxel, int* best_chunk) {
+  if (!e || trial_steps < 2) return VXG_E_ARG;
+  const int slot = 1023;
+  int rc = vxg_snapshot(e, slot);
+  if (rc) return rc;
+  const int cand[4] = {64, 128, 256, 512};
+  float best = 1e30f;
+  int bl = e->blk_link, bv = e->blk_voxel, bc = e->graph_chunk;
+  bool timing = e->timing;
+  e->timing = true;
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) {
+      e->blk_link = cand[a];
+      e->blk_voxel = cand[b];
+      int done = 0, div = 0;
+      if ((rc = vxg_step(e, trial_steps, dt, &done, &div))) break;
+      if ((rc = vxg_restore(e, slot))) break;
+      if (e->t_link + e->t_vox < best) {
+        best = e->t_link + e->t_vox;
+        bl = cand[a];
+        bv = cand[b];
+      }
+    }
+  e->timing = timing;
+  e->blk_link = bl;
+  e->blk_voxel = bv;
+  // graph chunk: replay throughput of a few candidate lengths
+  if (!rc) {
+    float bestc = 1e30f;
+    const int chunks[4] = {8, 32, 128, 512};
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    for (int k = 0; k < 4 && !rc; ++k) {
+      e->graph_chunk = chunks[k];
+      e->graph_valid = false;
+      int n = std::max(chunks[k], trial_steps), done = 0, div = 0;
+      if ((rc = vxg_step(e, chunks[k], dt, &done, &div))) break;  // capture outside the timing
+      cudaEventRecord(t0, e->stream);
+      if ((rc = vxg_step(e, n, dt, &done, &div))) break;
+      cudaEventRecord(t1, e->stream);
+      cudaEventSynchronize(t1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, t0, t1);
+      if (ms / n < bestc) { bestc = ms / n; bc = chunks[k]; }
+      if ((rc = vxg_restore(e, slot))) break;
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+  }
+  e->graph_chunk = bc;
+  e->graph_valid = false;
+  if (best_link) *best_link = bl;
+  if (best_voxel) *best_voxel = bv;
+  if (best_chunk) *best_chunk = bc;
+  if (e->precision == VXG_FP32C) e->stale64 = all_state_bits();
+  return rc;
 }
 
 int vxg_get_collisions(vxg_engine* e, int* pairs, int cap, int* n) {

@@ -234,3 +234,77 @@ class Sim:
         out = np.zeros((max(n, 1), 2), np.int32)
         self.f["get_collisions"](self.h, _ptr(out, C.c_int), n)
         return out[:n]
+
+
+# -- product extensions (include/vx_capi.h, "extensions for throughput users") --------------------
+_EXT_SIGS = {
+    "set_precision": (_i, [_p, _i]),
+    "read_positions": (_i, [_p, _dp]),
+    "set_temperatures": (_i, [_p, _fp]),
+    "state_info_device": (_f, [_p, _i, _i]),
+    "counters": (_i, [_p, C.POINTER(C.c_longlong), _i]),
+    "enable_timing": (_i, [_p, _i]),
+    "step_timing": (_i, [_p, _fp]),
+    "last_error": (C.c_char_p, [_p]),
+    "set_actuation": (_i, [_p, _i, _d, _d, _fp]),
+    "body_com": (_i, [_p, _ip, _i, _dp]),
+    "snapshot": (_i, [_p, _i]),
+    "restore": (_i, [_p, _i]),
+    "set_launch": (_i, [_p, _i, _i, _i]),
+    "autotune": (_i, [_p, _i, _f, _ip]),
+}
+
+ACT_OFF, ACT_UNIFORM, ACT_PER_VOXEL = 0, 1, 2
+
+
+class Engine:
+    """The product library's extensions on one :class:`Sim` (prefix ``vx``): precision mode,
+    per-step actuation, body centres of mass, device snapshots and launch tuning."""
+
+    def __init__(self, sim: Sim):
+        if sim.prefix != "vx":
+            raise ValueError("engine extensions exist on the product library only")
+        self.sim = sim
+        self.f = {}
+        for name, (res, args) in _EXT_SIGS.items():
+            fn = getattr(sim.lib, f"vx_{name}")
+            fn.restype = res
+            fn.argtypes = args
+            self.f[name] = fn
+
+    def _ck(self, rc):
+        if rc != 0:
+            raise RuntimeError(self.f["last_error"](self.sim.h).decode(errors="replace") or f"error {rc}")
+
+    def set_precision(self, mode: int):
+        self._ck(self.f["set_precision"](self.sim.h, mode))
+
+    def set_actuation(self, mode: int, amplitude: float = 0.0, frequency: float = 0.0, phase=None):
+        ph = None if phase is None else np.ascontiguousarray(phase, np.float32)
+        self._ck(self.f["set_actuation"](self.sim.h, mode, amplitude, frequency, _ptr(ph, C.c_float)))
+
+    def body_com(self, offsets) -> np.ndarray:
+        off = np.ascontiguousarray(offsets, np.int32)
+        out = np.zeros((len(off) - 1, 3), np.float64)
+        self._ck(self.f["body_com"](self.sim.h, _ptr(off, C.c_int), len(off) - 1, _ptr(out, C.c_double)))
+        return out
+
+    def snapshot(self, slot: int = 0):
+        self._ck(self.f["snapshot"](self.sim.h, slot))
+
+    def restore(self, slot: int = 0):
+        self._ck(self.f["restore"](self.sim.h, slot))
+
+    def set_launch(self, block_link: int = 0, block_voxel: int = 0, graph_chunk: int = 0):
+        self._ck(self.f["set_launch"](self.sim.h, block_link, block_voxel, graph_chunk))
+
+    def autotune(self, trial_steps: int = 20, dt: float = -1.0) -> tuple:
+        out = np.zeros(3, np.int32)
+        self._ck(self.f["autotune"](self.sim.h, trial_steps, dt, _ptr(out, C.c_int)))
+        return tuple(int(x) for x in out)
+
+    def read_positions(self) -> np.ndarray:
+        n = self.sim.voxel_count()
+        out = np.zeros(3 * n, np.float64)
+        self._ck(self.f["read_positions"](self.sim.h, _ptr(out, C.c_double)))
+        return out.reshape(3, n).T
