@@ -30,6 +30,7 @@ import os
 import subprocess
 import sys
 import tempfile
+import threading
 import time
 
 import numpy as np
@@ -49,18 +50,55 @@ def _dist():
 
 
 class _Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """SM clock and clock-event (throttle) reasons sampled during the timed region: NVML through
+    ctypes every ~2 ms (read-only queries), else ``nvidia-smi -lms 200``."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason bits
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+            0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, gpu: int):
         self.gpu = gpu
-        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.f = None
         self.p = None
+        self.nvml = None
+        self.samples = []
+        self.stop = threading.Event()
+        self.th = None
+
+    def _nvml_open(self):
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = C.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.gpu), C.byref(h)) != 0:
+                return None
+            fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            return lib, h, fn
+        except (OSError, AttributeError):
+            return None
+
+    def _poll(self):
+        lib, h, reasons_fn = self.nvml
+        mhz, mx, mask = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while not self.stop.is_set():
+            if (lib.nvmlDeviceGetClockInfo(h, 1, C.byref(mhz)) == 0 and
+                    lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0 and reasons_fn(h, C.byref(mask)) == 0):
+                self.samples.append((float(mhz.value), float(mx.value), int(mask.value)))
+            time.sleep(0.002)
 
     def __enter__(self):
+        self.nvml = self._nvml_open()
+        if self.nvml:
+            self.th = threading.Thread(target=self._poll, daemon=True)
+            self.th.start()
+            return self
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "200"],
@@ -70,30 +108,45 @@ class _Clocks:
         return self
 
     def __exit__(self, *a):
+        if self.th:
+            self.stop.set()
+            self.th.join()
         if self.p:
             self.p.terminate()
             self.p.wait()
 
     def summary(self):
-        self.f.flush()
-        self.f.seek(0)
         sm, mx, reasons = [], 0.0, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.f.read().splitlines():
-            p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
-                continue
-            try:
-                sm.append(float(p[1]))
-                mx = max(mx, float(p[2]))
-            except ValueError:
-                continue
-            for n, v in zip(names, p[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
+        if self.nvml:
+            for mhz, m, mask in self.samples:
+                sm.append(mhz)
+                mx = max(mx, m)
+                for bit, name in self.BITS.items():
+                    if mask & bit:
+                        reasons.add(name)
+            src = "nvml"
+        else:
+            src = "nvidia-smi"
+            if self.f:
+                self.f.flush()
+                self.f.seek(0)
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+                for line in self.f.read().splitlines():
+                    p = [x.strip() for x in line.split(",")]
+                    if len(p) < 9:
+                        continue
+                    try:
+                        sm.append(float(p[1]))
+                        mx = max(mx, float(p[2]))
+                    except ValueError:
+                        continue
+                    for n, v in zip(names, p[5:9]):
+                        if v.lower() == "active":
+                            reasons.add(n)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no clock samples"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "source": src}
 
 
 def _peak_hbm():
@@ -168,21 +221,26 @@ def run_reference(args, world, rank):
 
 
 def _timed(lib, sim, steps, dt, local, barrier):
-    """K steps with per-kernel CUDA events on the engine stream; returns timings and clocks."""
+    """K steps as they normally run (CUDA-graph replay), timed by one CUDA event pair on the engine
+    stream around the batch; then K more steps with per-pass events (no graphs) for the per-kernel
+    split.  Returns both and the clocks sampled during the first."""
     h = C.c_void_p(sim.h)
-    lib.vx_enable_timing(h, 1)
+    tm = (C.c_float * 4)()
+    lib.vx_enable_timing(h, 2)
     barrier()
     with _Clocks(local) as clk:
         done = sim.do_time_steps(steps, dt)
     barrier()
-    lib.vx_enable_timing(h, 0)
     if done != steps:
         raise RuntimeError(f"diverged after {done} steps")
-    tm = (C.c_float * 4)()
     lib.vx_step_timing(h, tm)
-    batch_ms, link_ms, col_ms, vox_ms = [float(x) for x in tm]
-    # first kernel to last kernel of the batch, extended by one step's share of the gap
-    total_ms = batch_ms * steps / max(steps - 1, 1) if steps > 1 else link_ms + col_ms + vox_ms
+    total_ms = float(tm[0])
+    lib.vx_enable_timing(h, 1)
+    if sim.do_time_steps(steps, dt) != steps:
+        raise RuntimeError("diverged in the per-pass timing run")
+    lib.vx_enable_timing(h, 0)
+    lib.vx_step_timing(h, tm)
+    _, link_ms, col_ms, vox_ms = [float(x) for x in tm]
     return {"total_ms": total_ms, "link_ms": link_ms, "collide_ms": col_ms, "voxel_ms": vox_ms, "clocks": clk.summary()}
 
 
@@ -256,7 +314,8 @@ def run_ours(args, world, rank, local):
     achieved = b[kernel] / (k_ms / 1e3) / 1e9
     peak, peak_kind = _peak_hbm()
     kname = f"k_{kernel}{'32' if fp32 else ''}"
-    roof = {"bound": "hbm", "kernel": f"{kname} ({'FP32C' if fp32 else 'FP64'} {kernel} pass)", "achieved": achieved,
+    label = f"k_poisson + {kname}" if kernel == "link" else kname
+    roof = {"bound": "hbm", "kernel": f"{label} ({'FP32C' if fp32 else 'FP64'} {kernel} pass)", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": b[kernel], "ms_per_launch": k_ms,
             "traffic": _traffic(f"{kname}_{'fp32c' if fp32 else 'fp64'}", nv, nl),

@@ -188,10 +188,12 @@ int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* 
 /* Full device-side copies of the simulation state (checkpoint / restart). */
 int vxg_snapshot(vxg_engine* e, int slot);
 int vxg_restore(vxg_engine* e, int slot);
-/* Timing mode: vxg_step records CUDA events on the engine stream around the link pass (with the
- * Poisson pre-pass), the collision stage and the voxel pass of every step (no graph replay).
- * vxg_last_step_timing gives the per-step averages of the last batch in milliseconds,
- * vxg_last_batch_ms the device time from its first to its last kernel. */
+/* Timing mode 1: vxg_step records CUDA events on the engine stream around the link pass (with the
+ * Poisson pre-pass), the collision stage and the voxel pass of every step (no graph replay);
+ * vxg_last_step_timing gives the per-step averages of the last batch in milliseconds and
+ * vxg_last_batch_ms the device time from its first to its last kernel.  Mode 2: one event pair
+ * around the whole batch as it normally runs (graph replay included); vxg_last_batch_ms gives
+ * its device time.  Mode 0: off. */
 int vxg_enable_timing(vxg_engine* e, int on);
 int vxg_last_step_timing(vxg_engine* e, float* ms_link, float* ms_collide, float* ms_voxel);
 int vxg_last_batch_ms(vxg_engine* e, float* ms);

@@ -37,6 +37,7 @@ struct View {
   float* d;         // 3 nv displacement from the lattice origin
   float* c;         // 3 nv Kahan compensation (true displacement = d - c)
   float* q;         // 4 nv orientation
+  float* qc;        // 4 nv Kahan compensation of the orientation (true orientation = q - qc)
   float* lin;       // 3 nv linear momentum
   float* ang;       // 3 nv angular momentum
   float* pos2;      // 3 nl (x holds the extension pos2.x - L, as in the reference's state)
@@ -99,6 +100,24 @@ VX_HD q4 from_rotation_vector(const f3& in) {
     s = sinf(m) / m;
   }
   return Q4(w, th.x * s, th.y * s, th.z * s);
+}
+// The same rotation as from_rotation_vector, returned as its difference from the identity quaternion
+// (w - 1, x, y, z): the orientation update q' = dq q is then q + (dq - 1) q, a small increment that
+// is added with compensation.  w - 1 is formed without cancellation.
+VX_HD q4 rotation_increment(const f3& in) {
+  f3 th = F3(0.5f * in.x, 0.5f * in.y, 0.5f * in.z);
+  float m2 = th.x * th.x + th.y * th.y + th.z * th.z;
+  float wm1, s;
+  if (m2 < 1e-6f) {
+    wm1 = -0.5f * m2 + m2 * m2 * (1.0f / 24.0f);
+    s = 1.0f - m2 * (1.0f / 6.0f) + m2 * m2 * (1.0f / 120.0f);
+  } else {
+    float m = sqrtf(m2);
+    float h = sinf(0.5f * m);
+    wm1 = -2.0f * h * h;  // cos m - 1
+    s = sinf(m) / m;
+  }
+  return Q4(wm1, th.x * s, th.y * s, th.z * s);
 }
 VX_HD void from_angle_to_pos_x(q4& q, const f3& r) {
   if (r.x == 0 && r.y == 0 && r.z == 0) return;
@@ -314,13 +333,14 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
     st3(S.d, nv, v, F3((float)e->translation[0], (float)e->translation[1], (float)e->translation[2]));
     st3(S.c, nv, v, F3(0, 0, 0));
     stq(S.q, nv, v, Q4((float)e->rotq[0], (float)e->rotq[1], (float)e->rotq[2], (float)e->rotq[3]));
+    stq(S.qc, nv, v, Q4(0, 0, 0, 0));
     st3(S.lin, nv, v, F3(0, 0, 0));
     st3(S.ang, nv, v, F3(0, 0, 0));
     return;
   }
   uint32_t flags = B.vflags[v];
   f3 d = ld3(S.d, nv, v), c = ld3(S.c, nv, v), lin = ld3(S.lin, nv, v), ang = ld3(S.ang, nv, v);
-  q4 q = ldq(S.q, nv, v);
+  q4 q = ldq(S.q, nv, v), qc = ldq(S.qc, nv, v);
   int lk[6];
 #pragma unroll
   for (int i = 0; i < 6; ++i) lk[i] = B.vlinks[i * nv + v];
@@ -403,7 +423,13 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   }
   ang.x += dt * M.x; ang.y += dt * M.y; ang.z += dt * M.z;
   float dti = dt * m.inertiaInv;
-  q = qmul(from_rotation_vector(F3(dti * ang.x, dti * ang.y, dti * ang.z)), q);
+  {
+    q4 dq = qmul(rotation_increment(F3(dti * ang.x, dti * ang.y, dti * ang.z)), q);
+    kahan_add(q.w, qc.w, dq.w);
+    kahan_add(q.x, qc.x, dq.x);
+    kahan_add(q.y, qc.y, dq.y);
+    kahan_add(q.z, qc.z, dq.z);
+  }
   if (e) {
     if (e->dof & 1) { d.x = (float)e->translation[0]; c.x = 0; lin.x = 0; }
     if (e->dof & 2) { d.y = (float)e->translation[1]; c.y = 0; lin.y = 0; }
@@ -411,6 +437,7 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
     if (e->dof & 56) {
       if ((e->dof & 56) == 56) {
         q = Q4((float)e->rotq[0], (float)e->rotq[1], (float)e->rotq[2], (float)e->rotq[3]);
+        qc = Q4(0, 0, 0, 0);
         ang = F3(0, 0, 0);
       } else {
         f3 r = to_rotation_vector(q);
@@ -418,6 +445,7 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
         if (e->dof & 16) { r.y = 0; ang.y = 0; }
         if (e->dof & 32) { r.z = 0; ang.z = 0; }
         q = from_rotation_vector(r);
+        qc = Q4(0, 0, 0, 0);
       }
     }
   }
@@ -426,6 +454,7 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   st3(S.lin, nv, v, lin);
   st3(S.ang, nv, v, ang);
   stq(S.q, nv, v, q);
+  stq(S.qc, nv, v, qc);
   B.vflags[v] = (flags & ~(uint32_t)VXG_VF_STATIC_FRICTION) | (staticF ? VXG_VF_STATIC_FRICTION : 0u) |
                 VXG_VF_PSTRAIN_INVALID;
 }

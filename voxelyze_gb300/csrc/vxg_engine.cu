@@ -255,7 +255,19 @@ __global__ void k_conv(vx32::View S, double s, int field, int to32) {
         }
       break;
     case VXG_F_LINMOM: cv(B.linMom, S.lin, 3, nv); break;
-    case VXG_F_ORIENT: cv(B.orient, S.q, 4, nv); break;
+    case VXG_F_ORIENT:
+      if (i < nv)
+        for (int k = 0; k < 4; ++k) {
+          if (to32) {
+            double q64 = B.orient[k * nv + i];
+            float q = (float)q64;
+            S.q[k * nv + i] = q;
+            S.qc[k * nv + i] = (float)((double)q - q64);  // true orientation = q - qc
+          } else {
+            B.orient[k * nv + i] = (double)S.q[k * nv + i] - (double)S.qc[k * nv + i];
+          }
+        }
+      break;
     case VXG_F_ANGMOM: cv(B.angMom, S.ang, 3, nv); break;
     case VXG_F_PREV_DT:
       if (to32) { if (i == 0 && nv) B.ctl->last_dt = B.prevDt[0]; }
@@ -401,7 +413,8 @@ struct vxg_engine {
   vxg_globals g{};
   bool have_globals = false;
   Collide col;
-  bool timing = false;
+  int timing = 0;                 // 0 off, 1 per-pass events every step, 2 one event pair per batch
+  cudaEvent_t bev[2] = {nullptr, nullptr};
   cudaEvent_t ev[4] = {};
   std::vector<cudaEvent_t> tev;  // timing mode: 4 events per step of the last batch
   int tev_used = 0;
@@ -597,6 +610,7 @@ int vxg_destroy(vxg_engine* e) {
   for (int i = 0; i < 4; ++i)
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);
   for (cudaEvent_t x : e->tev) cudaEventDestroy(x);
+  for (cudaEvent_t x : e->bev) if (x) cudaEventDestroy(x);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return VXG_OK;
@@ -625,14 +639,14 @@ int vxg_resize(vxg_engine* e, int nv, int nl) {
   e->arena_bytes = total;
   for (int f = 0; f < VXG_F_TIME; ++f) e->field_ptr[f] = e->arena + off[f];
   if (e->precision == VXG_FP32C) {
-    size_t vb = ((sizeof(float) * 16 * (size_t)nv + 255) / 256) * 256;
+    size_t vb = ((sizeof(float) * 20 * (size_t)nv + 255) / 256) * 256;
     size_t lb = ((sizeof(float) * 22 * (size_t)nl + 255) / 256) * 256;
     e->arena32_bytes = std::max<size_t>(vb + lb, 256);
     VXG_CK(cudaMalloc(&e->arena32, e->arena32_bytes));
     VXG_CK(cudaMemsetAsync(e->arena32, 0, vb + lb, e->stream));
     float* p = (float*)e->arena32;
     e->V.d = p; e->V.c = p + 3 * (size_t)nv; e->V.q = p + 6 * (size_t)nv;
-    e->V.lin = p + 10 * (size_t)nv; e->V.ang = p + 13 * (size_t)nv;
+    e->V.lin = p + 10 * (size_t)nv; e->V.ang = p + 13 * (size_t)nv; e->V.qc = p + 16 * (size_t)nv;
     float* L = (float*)(e->arena32 + vb);
     e->V.pos2 = L; e->V.a1v = L + 3 * (size_t)nl; e->V.a2v = L + 6 * (size_t)nl; e->V.fN = L + 9 * (size_t)nl;
     e->V.fP = L + 12 * (size_t)nl; e->V.mN = L + 15 * (size_t)nl; e->V.mP = L + 18 * (size_t)nl;
@@ -811,7 +825,12 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
   unsigned z2[2] = {0u, 0u};
   VXG_CK(cudaMemcpyAsync(e->ctl->maxf, z2, sizeof(z2), cudaMemcpyHostToDevice, e->stream));
-  bool use_graph = !e->timing && nsteps > 1;
+  bool use_graph = e->timing != 1 && nsteps > 1;
+  if (e->timing == 2) {
+    for (int k = 0; k < 2; ++k)
+      if (!e->bev[k]) VXG_CK(cudaEventCreate(&e->bev[k]));
+    VXG_CK(cudaEventRecord(e->bev[0], e->stream));
+  }
   e->tev_used = 0;
   if (use_graph) {
     int chunk = e->graph_chunk;
@@ -840,7 +859,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
       }
       VXG_CK(cudaGraphLaunch(e->graph, e->stream));
     }
-  } else if (e->timing) {
+  } else if (e->timing == 1) {
     size_t need = (size_t)4 * nsteps;
     while (e->tev.size() < need) {
       cudaEvent_t x;
@@ -852,11 +871,13 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   } else {
     for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1);
   }
+  if (e->timing == 2) VXG_CK(cudaEventRecord(e->bev[1], e->stream));
   int h[4];
   VXG_CK(cudaMemcpyAsync(h, e->ctl, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
   VXG_CK(cudaGetLastError());
-  if (e->timing && e->tev_used > 0) {
+  if (e->timing == 2) VXG_CK(cudaEventElapsedTime(&e->t_batch, e->bev[0], e->bev[1]));
+  if (e->timing == 1 && e->tev_used > 0) {
     double a = 0, b = 0, c = 0;
     for (int s = 0; s < e->tev_used; ++s) {
       float x = 0, y = 0, z = 0;
@@ -1080,8 +1101,8 @@ int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* 
   const int cand[4] = {64, 128, 256, 512};
   float best = 1e30f;
   int bl = e->blk_link, bv = e->blk_voxel, bc = e->graph_chunk;
-  bool timing = e->timing;
-  e->timing = true;
+  int timing = e->timing;
+  e->timing = 1;
   for (int a = 0; a < 4; ++a)
     for (int b = 0; b < 4; ++b) {
       e->blk_link = cand[a];
@@ -1152,7 +1173,8 @@ int vxg_counters(vxg_engine* e, long long* out, int n) {
 
 int vxg_enable_timing(vxg_engine* e, int on) {
   if (!e) return VXG_E_ARG;
-  e->timing = on != 0;
+  if (on < 0 || on > 2) return VXG_E_ARG;
+  e->timing = on;
   return VXG_OK;
 }
 

@@ -41,19 +41,21 @@ def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
 #                         8 written, strain/maxStrain/strainOffset 12 read + 16 written, forces and
 #                         moments 48 written                                              = 188 B
 #             per voxel : displacement 12, orientation 16, material id 4                  =  32 B
-#   voxel pass, per voxel: displacement, compensation, orientation, momenta 64 read + 64 written,
-#                         flags 4+4, material id 4, external id 4, 6 link ids 24, lattice z 4,
-#                         temperature 4                                                  = 176 B
+#                         (+ the cached Poisson strain 12 when nu != 0)
+#   voxel pass, per voxel: displacement and orientation with their compensations, momenta 80 read
+#                         + 80 written, flags 4+4, material id 4, external id 4, 6 link ids 24,
+#                         lattice z 4, temperature 4                                     = 208 B
 #             per link  : the force and moment each end gathers, 2 x 24                   =  48 B
 FP32C_LINK_PER_LINK = 188
 FP32C_LINK_PER_VOXEL = 32
-FP32C_VOXEL_PER_VOXEL = 176
+FP32C_LINK_PER_VOXEL_POISSON = 12
+FP32C_VOXEL_PER_VOXEL = 208
 FP32C_VOXEL_PER_LINK = 48
 
 
 def fp32c_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
     link = FP32C_LINK_PER_LINK * n_links + FP32C_LINK_PER_VOXEL * n_voxels
     if poisson:
-        link += FP64_POISSON_PER_VOXEL * n_voxels + FP64_POISSON_PER_LINK * n_links
+        link += (FP64_POISSON_PER_VOXEL + FP32C_LINK_PER_VOXEL_POISSON) * n_voxels + FP64_POISSON_PER_LINK * n_links
     voxel = FP32C_VOXEL_PER_VOXEL * n_voxels + FP32C_VOXEL_PER_LINK * n_links
     return {"link": link, "voxel": voxel, "step": link + voxel}
