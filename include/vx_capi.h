@@ -52,6 +52,21 @@ int vx_set_precision(void* s, int mode);                    /* 0 = FP64 (default
 int vx_read_positions(void* s, double* xyz);                /* 3 n_voxels doubles, component-major, straight from the GPU */
 int vx_set_temperatures(void* s, const float* t);           /* n_voxels floats: every voxel's setTemperature */
 float vx_state_info_device(void* s, int info, int type);    /* GPU reduction, see vxg_reduce */
+/* stateInfo (info, type as vx_state_info; not PRESSURE) reduced on the GPU and written as one float
+ * to d_out, a pointer into device memory of the simulation's device; no counterpart in the
+ * reference, whose stateInfo (src/Voxelyze.cpp:752-800) is a host loop.  For callers that may not
+ * allocate: a control loop reading the state every step, which must not stall on an allocation's
+ * implicit synchronisation, or a process whose device memory is held by another allocator.  This
+ * call allocates no device or host memory and does not synchronise: the value is ready once the
+ * simulation's stream (vxg_stream) reaches it.  Partial results live in a fixed scratch array in
+ * the library (24 KB per device), so at most 4,194,304 voxels or links are reduced; larger counts
+ * return VXG_E_SIZE.  Its completion counter starts at zero when the library loads and each call
+ * leaves it at zero.  The first call on a device looks the scratch up and may make the CUDA runtime
+ * load this library's device code: make it before any stream capture.  Calls that overlap in time
+ * on one device (several threads, streams or simulations) share the scratch and race: serialise
+ * them.  Host edits not yet on the device are refused (VXG_E_STATE), not uploaded.  Returns 0, or
+ * a VXG_E_* code with a static message in *why (why may be NULL). */
+int vx_state_info_into(void* s, int info, int type, float* d_out, const char** why);
 int vx_counters(void* s, long long* out, int n);            /* vxg_counters of the engine */
 int vx_enable_timing(void* s, int on);                      /* vxg_enable_timing */
 int vx_step_timing(void* s, float* out4);                   /* batch ms, link/collide/voxel ms per step */

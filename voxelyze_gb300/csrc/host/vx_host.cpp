@@ -1312,6 +1312,15 @@ int vx_set_temperatures(void* s, const float* t) { return H(s)->vx.setTemperatur
 float vx_state_info_device(void* s, int info, int type) {
   return H(s)->vx.stateInfoDevice((CVoxelyze::stateInfoType)info, (CVoxelyze::valueType)type);
 }
+int vx_state_info_into(void* s, int info, int type, float* d_out, const char** why) {
+  // No flush here: uploading pending host edits may allocate, so they are refused instead.
+  VxImpl& I = *H(s)->vx.impl();
+  if (!I.eng || I.topo_dirty || I.tables_dirty || I.state_dirty || I.act_dirty) {
+    if (why) *why = "vx_state_info_into: host edits are not on the device yet (step or upload first)";
+    return VXG_E_STATE;
+  }
+  return vxg_reduce_fixed(I.eng, info, type, d_out, why);
+}
 int vx_counters(void* s, long long* out, int n) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.impl()->eng) return -1;

@@ -10,6 +10,11 @@
 
 #include "vxg.h"
 
+// vxg_engine.cu: stateInfo reduction into caller device memory through fixed device scratch
+// (library-internal; exposed as vx_state_info_into)
+__attribute__((visibility("hidden"))) int vxg_reduce_fixed(vxg_engine* e, int info, int type, float* d_out,
+                                                          const char** why);
+
 class CVoxelyze;
 class CVX_Voxel;
 class CVX_Link;

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -186,6 +187,64 @@ __global__ void k_reduce(View S, int info, int n, double* out /* 3 per block: mi
     out[3 * blockIdx.x + 1] = mx;
     out[3 * blockIdx.x + 2] = sm;
   }
+}
+
+// ---- the same reduction into caller memory with a fixed scratch array -------------------------
+// Block b reduces elements [b * kFixedSpan, (b + 1) * kFixedSpan); its min, max and sum go to
+// slots 3b..3b+2 of the scratch; the block that finishes last (the completion counter after the
+// partials) folds the partials in block order, writes the result and sets the counter back to 0.
+constexpr int kFixedBlocks = 1024;                // partial slots
+constexpr int kFixedItems = 16;                   // elements per thread
+constexpr int kFixedSpan = kBlock * kFixedItems;  // elements per block
+constexpr long long kFixedMaxElements = (long long)kFixedBlocks * kFixedSpan;  // 4,194,304
+// 24 KB + the counter.  Zero when the module loads, and zero again at the end of every call.
+static __device__ __align__(256) double g_fixed_scratch[3 * kFixedBlocks + 2];
+
+__global__ void k_reduce_fixed(View S, int info, int n, int type, double* scratch, float* out) {
+  __shared__ double smin[kBlock / 32], smax[kBlock / 32], ssum[kBlock / 32];
+  __shared__ int last;
+  double mn = 3.4e38, mx = -3.4e38, sm = 0.0;
+  const int base = blockIdx.x * kFixedSpan;
+  for (int k = 0; k < kFixedItems; ++k) {
+    int i = base + k * kBlock + threadIdx.x;
+    if (i < n) {
+      float t = info_value(S, info, i);
+      mn = t < mn ? t : mn;
+      mx = t > mx ? t : mx;
+      sm += t;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    sm += __shfl_xor_sync(0xffffffffu, sm, o);
+  }
+  int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { smin[w] = mn; smax[w] = mx; ssum[w] = sm; }
+  __syncthreads();
+  unsigned* done = reinterpret_cast<unsigned*>(scratch + 3 * kFixedBlocks);
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < kBlock / 32; ++k) { mn = fmin(mn, smin[k]); mx = fmax(mx, smax[k]); sm += ssum[k]; }
+    scratch[3 * blockIdx.x] = mn;
+    scratch[3 * blockIdx.x + 1] = mx;
+    scratch[3 * blockIdx.x + 2] = sm;
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  const volatile double* part = scratch;
+  double a = part[0], b = part[1], c = 0.0;
+  for (unsigned k = 0; k < gridDim.x; ++k) {
+    a = fmin(a, part[3 * k]);
+    b = fmax(b, part[3 * k + 1]);
+    c += part[3 * k + 2];
+  }
+  *out = type == 0 ? (float)a : type == 1 ? (float)b : type == 2 ? (float)c : (float)(c / n);
+  *done = 0u;
+  __threadfence();
 }
 
 int grid_for(int n) { return std::max(1, (n + kBlock - 1) / kBlock); }
@@ -563,6 +622,74 @@ static int upload_table(vxg_engine* e, T** dptr, int* have, const T* src, int n)
   if (n) {
     cudaError_t c = cudaMemcpyAsync(*dptr, src, sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, e->stream);
     if (c != cudaSuccess) return fail(e, VXG_E_CUDA, "table copy", c);
+  }
+  return VXG_OK;
+}
+
+// ---- fixed-scratch set-up: one device address per device, looked up once -------------------
+namespace {
+std::mutex g_fixed_mu;
+constexpr int kFixedMaxDevices = 64;
+double* g_fixed_addr[kFixedMaxDevices] = {};
+}  // namespace
+
+// Same quantity as vxg_reduce, written to d_out (device memory) on the engine's stream, through
+// the fixed scratch above: no device or host memory is allocated, nothing is synchronised.  The
+// first call on a device looks the scratch up with cudaGetSymbolAddress, which may load this
+// library's device code and so allocate inside the CUDA runtime: make that first call before any
+// stream capture.  All calls on one device share the scratch: calls that overlap in time (several
+// host threads or streams, several engines on one device) race and must be serialised by the
+// caller.  Errors return a code and a static message in *why; nothing is written to d_out then.
+__attribute__((visibility("hidden"))) int vxg_reduce_fixed(vxg_engine* e, int info, int type, float* d_out,
+                                                          const char** why) {
+  const char* dummy = nullptr;
+  if (!why) why = &dummy;
+  *why = nullptr;
+  if (!e || !d_out || info < 0 || info > 9 || type < 0 || type > 3) {
+    *why = "vx_state_info_into: bad engine, output pointer, info or type";
+    return VXG_E_ARG;
+  }
+  if (info == 8) {
+    *why = "vx_state_info_into: PRESSURE is reduced on the host";
+    return VXG_E_ARG;
+  }
+  const bool link = info == 5 || info == 6 || info == 7;
+  const long long n = link ? e->nl : e->nv;
+  if (n > kFixedMaxElements) {
+    *why = "vx_state_info_into: more elements than the fixed scratch covers (at most 4,194,304 voxels or links)";
+    return VXG_E_SIZE;
+  }
+  if (cudaSetDevice(e->device) != cudaSuccess || e->device < 0 || e->device >= kFixedMaxDevices) {
+    *why = "vx_state_info_into: cannot make the engine's device current";
+    return VXG_E_CUDA;
+  }
+  double* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_fixed_mu);
+    if (!g_fixed_addr[e->device]) {
+      void* p = nullptr;
+      cudaError_t c = cudaGetSymbolAddress(&p, g_fixed_scratch);  // with e->device current
+      if (c != cudaSuccess || !p) {
+        *why = "vx_state_info_into: cudaGetSymbolAddress of the fixed scratch failed";
+        return VXG_E_CUDA;
+      }
+      g_fixed_addr[e->device] = static_cast<double*>(p);
+    }
+    scratch = g_fixed_addr[e->device];
+  }
+  if (n == 0) {
+    if (cudaMemsetAsync(d_out, 0, sizeof(float), e->stream) != cudaSuccess) {
+      *why = "vx_state_info_into: cudaMemsetAsync failed";
+      return VXG_E_CUDA;
+    }
+    return VXG_OK;
+  }
+  ensure64(e);
+  const int blocks = (int)((n + kFixedSpan - 1) / kFixedSpan);
+  k_reduce_fixed<<<blocks, kBlock, 0, e->stream>>>(e->S, info, (int)n, type, scratch, d_out);
+  if (cudaGetLastError() != cudaSuccess) {
+    *why = "vx_state_info_into: kernel launch failed";
+    return VXG_E_CUDA;
   }
   return VXG_OK;
 }
