@@ -156,16 +156,6 @@ def _peak_hbm():
         return 6800.0, "fallback"
 
 
-def _traffic(kernel: str, n_voxels: int, n_links: int):
-    """DRAM bytes per launch from the committed ncu capture (profiles/traffic.json), scaled by
-    the units one launch processes; None when no capture is committed."""
-    try:
-        t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))[kernel]
-        return t["bytes_per_voxel"] * n_voxels + t["bytes_per_link"] * n_links
-    except Exception:
-        return None
-
-
 DIMS = (128, 128, 64)
 
 
@@ -318,7 +308,7 @@ def run_ours(args, world, rank, local):
     roof = {"bound": "hbm", "kernel": f"{label} ({'FP32C' if fp32 else 'FP64'} {kernel} pass)", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": b[kernel], "ms_per_launch": k_ms,
-            "traffic": _traffic(f"{kname}_{'fp32c' if fp32 else 'fp64'}", nv, nl),
+            "traffic": R.measured_traffic(f"{'fp32c' if fp32 else 'fp64'}_{kernel}", nv, nl),
             "step_bytes": b["step"], "step_frac": b["step"] / (t_head["total_ms"] / args.steps / 1e3) / 1e9 / peak}
 
     cpu = None

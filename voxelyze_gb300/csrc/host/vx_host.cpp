@@ -86,6 +86,7 @@ void CVoxelyze::clear() {  // Voxelyze.cpp:323-355
   voxelMats.clear();
   for (CVX_MaterialLink* m : linkMats) delete m;
   linkMats.clear();
+  pimpl->link_mat_of.clear();
   for (CVX_Collision* c : collisionsList) delete c;
   collisionsList.clear();
   ambientTemp = 0.0f;
@@ -146,6 +147,7 @@ bool CVoxelyze::removeMaterial(CVX_Material* toRemove) {  // Voxelyze.cpp:384-40
         auto& d = o->dependentMaterials;
         d.erase(std::remove(d.begin(), d.end(), (CVX_Material*)*it), d.end());
       }
+      pimpl->link_mat_of.erase(VxImpl::mat_pair((*it)->vox1Mat, (*it)->vox2Mat));
       delete *it;
       it = linkMats.erase(it);
     } else {
@@ -168,9 +170,12 @@ bool CVoxelyze::replaceMaterial(CVX_Material* a, CVX_Material* b) {  // Voxelyze
 }
 
 CVX_MaterialLink* CVoxelyze::combinedMaterial(CVX_MaterialVoxel* m1, CVX_MaterialVoxel* m2) {
-  for (CVX_MaterialLink* m : linkMats)
-    if ((m->vox1Mat == m1 && m->vox2Mat == m2) || (m->vox1Mat == m2 && m->vox2Mat == m1)) return m;
+  // Voxelyze.cpp:628-640: the first existing link material of this pair, else a new one
+  auto key = VxImpl::mat_pair(m1, m2);
+  auto it = pimpl->link_mat_of.find(key);
+  if (it != pimpl->link_mat_of.end()) return it->second;
   CVX_MaterialLink* n = new CVX_MaterialLink(m1, m2);
+  pimpl->link_mat_of.emplace(key, n);
   n->owner = this;
   linkMats.push_back(n);
   m1->dependentMaterials.push_back(n);

@@ -55,6 +55,18 @@ struct VxImpl {
   std::vector<float> act_phase;
   bool act_dirty = false;
   std::map<float, int> powf_slots;  // exponent -> table slot already on the device
+  // combined link material of an (unordered) pair of voxel materials: the reference searches the
+  // link-material list linearly, which is quadratic when every voxel has its own material
+  struct PairHash {
+    size_t operator()(const std::pair<const void*, const void*>& p) const {
+      size_t a = reinterpret_cast<size_t>(p.first), b = reinterpret_cast<size_t>(p.second);
+      return a * 0x9E3779B97F4A7C15ull ^ (b + 0x7F4A7C159E3779B9ull + (a << 6) + (a >> 2));
+    }
+  };
+  std::unordered_map<std::pair<const void*, const void*>, CVX_MaterialLink*, PairHash> link_mat_of;
+  static std::pair<const void*, const void*> mat_pair(const void* a, const void* b) {
+    return a < b ? std::make_pair(a, b) : std::make_pair(b, a);
+  }
   std::string err;
 
   static uint64_t key(int x, int y, int z) {

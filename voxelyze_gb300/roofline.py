@@ -59,3 +59,18 @@ def fp32c_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
         link += (FP64_POISSON_PER_VOXEL + FP32C_LINK_PER_VOXEL_POISSON) * n_voxels + FP64_POISSON_PER_LINK * n_links
     voxel = FP32C_VOXEL_PER_VOXEL * n_voxels + FP32C_VOXEL_PER_LINK * n_links
     return {"link": link, "voxel": voxel, "step": link + voxel}
+
+
+# DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
+# 128x128x64 lattice, FP32C, warm step (profiles/fp32c_lattice128x128x64_dram.md), per unit
+MEASURED_TRAFFIC = {
+    "fp32c_link": {"per_voxel": 56.2, "per_link": 175.1},   # k_poisson + k_link32
+    "fp32c_voxel": {"per_voxel": 290.2, "per_link": 0.0},   # k_voxel32
+}
+
+
+def measured_traffic(kind: str, n_voxels: int, n_links: int):
+    t = MEASURED_TRAFFIC.get(kind)
+    if t is None:
+        return None
+    return t["per_voxel"] * n_voxels + t["per_link"] * n_links
