@@ -77,6 +77,10 @@ int vx_set_actuation(void* s, int mode, double amplitude, double frequency, cons
 int vx_body_com(void* s, const int* offsets, int n_bodies, double* out);   /* vxg_body_com */
 int vx_snapshot(void* s, int slot);                         /* vxg_snapshot: device checkpoint */
 int vx_restore(void* s, int slot);                          /* vxg_restore (same scene only) */
+/* gradient of the per-body centre-of-mass x after nsteps with respect to every voxel's E, density
+ * and actuation phase: vxg_adjoint_com_x (no counterpart in the reference) */
+int vx_adjoint_com_x(void* s, int nsteps, float dt, int checkpoint_every, const int* body_offsets, int n_bodies,
+                     double* objective, double* dE, double* drho, double* dphase);
 int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk); /* vxg_set_launch */
 int vx_autotune(void* s, int trial_steps, float dt, int* out3);            /* vxg_autotune: link, voxel, chunk */
 

@@ -185,6 +185,20 @@ int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_
 /* Times short runs of the current scene for every block-size pair and several graph lengths and
  * keeps the fastest; the state is restored afterwards. */
 int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* best_voxel, int* best_chunk);
+/* Differentiated run of the FP64 path (no counterpart in the reference).  Runs nsteps steps of
+ * length dt from the current state (the engine ends in the same state as after vxg_step) and
+ * returns, per body (voxel ranges [body_offsets[b], body_offsets[b+1])), the mass-weighted centre
+ * of mass x after the last step, and the gradient of the sum of those objectives with respect to
+ * every voxel's material Young's modulus (dE), density (drho) and per-voxel actuation phase
+ * (dphase, actuation mode 2), each n_voxels doubles (NULL to skip).  Gradients are taken per voxel:
+ * with one material per voxel they are the derivatives with respect to that material's E and rho.
+ * Reverse mode with hand-written adjoint kernels; the state is checkpointed every checkpoint_every
+ * steps and each segment is recomputed once, so device memory grows with checkpoint_every.
+ * Scope: linear materials with Poisson's ratio 0 and no failure strain, no collisions, externals
+ * that fix all or none of the degrees of freedom, links in the small-angle branch; floor contact
+ * and friction are differentiated along the branch the forward run took. */
+int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every, const int* body_offsets,
+                      int n_bodies, double* objective, double* dE, double* drho, double* dphase);
 /* Full device-side copies of the simulation state (checkpoint / restart). */
 int vxg_snapshot(vxg_engine* e, int slot);
 int vxg_restore(vxg_engine* e, int slot);

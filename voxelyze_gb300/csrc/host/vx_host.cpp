@@ -1378,6 +1378,16 @@ int vx_restore(void* s, int slot) {
   vx.impl()->device_ahead = true;
   return 0;
 }
+int vx_adjoint_com_x(void* s, int nsteps, float dt, int checkpoint_every, const int* body_offsets, int n_bodies,
+                     double* objective, double* dE, double* drho, double* dphase) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  int rc = vxg_adjoint_com_x(vx.impl()->eng, nsteps, dt, checkpoint_every, body_offsets, n_bodies, objective, dE, drho,
+                             dphase);
+  vx.impl()->device_ahead = true;
+  if (rc) { vx.impl()->err = vxg_last_error(vx.impl()->eng); return -1; }
+  return 0;
+}
 int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.upload()) return -1;

@@ -446,6 +446,7 @@ static FieldDesc field_desc(int f) {
 }
 
 #include "vxg_collide.cuh"
+#include "vxg_adjoint.cuh"
 
 struct vxg_engine {
   int device = 0;
@@ -472,6 +473,8 @@ struct vxg_engine {
   vxg_globals g{};
   bool have_globals = false;
   Collide col;
+  // whether the scene is inside the differentiated scope (set with the tables)
+  const char* adj_scope = "no tables";
   int timing = 0;                 // 0 off, 1 per-pass events every step, 2 one event pair per batch
   cudaEvent_t bev[2] = {nullptr, nullptr};
   cudaEvent_t ev[4] = {};
@@ -836,6 +839,15 @@ int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const 
   if ((rc = upload_table(e, &e->d_vm, &e->n_vm, vm, n_vm))) return rc;
   if ((rc = upload_table(e, &e->d_lm, &e->n_lm, lm, n_lm))) return rc;
   if ((rc = upload_table(e, &e->d_ext, &e->n_ext, ext, n_ext))) return rc;
+  e->adj_scope = nullptr;
+  for (int k = 0; k < n_lm && !e->adj_scope; ++k)
+    if (!lm[k].linear || lm[k].nu != 0.0f || lm[k].epsilonFail != -1.0f)
+      e->adj_scope = "a link material is not linear, has Poisson's ratio != 0 or a failure strain";
+  for (int k = 0; k < n_vm && !e->adj_scope; ++k)
+    if (vm[k].nu != 0.0f) e->adj_scope = "a voxel material has Poisson's ratio != 0";
+  for (int k = 0; k < n_ext && !e->adj_scope; ++k)
+    if ((ext[k].dof & 0x3F) != 0 && (ext[k].dof & 0x3F) != 0x3F)
+      e->adj_scope = "an external fixes some but not all degrees of freedom";
   VXG_CK(cudaStreamSynchronize(e->stream));
   rebuild_view(e);
   return VXG_OK;
@@ -1022,6 +1034,108 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   if (steps_done) *steps_done = h[2];
   if (diverged) *diverged = h[1] ? 1 : 0;
   if (h[3]) return fail(e, VXG_E_DEVICE_STATUS, e->col.status_message(h[3]));
+  return VXG_OK;
+}
+
+// ---- differentiated run ---------------------------------------------------------------------
+int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every, const int* body_offsets,
+                      int n_bodies, double* objective, double* dE, double* drho, double* dphase) {
+  if (!e || nsteps <= 0 || !(dt > 0.0f) || checkpoint_every <= 0 || !body_offsets || n_bodies <= 0 || !objective)
+    return VXG_E_ARG;
+  if (!e->have_globals) return fail(e, VXG_E_STATE, "vxg_set_globals was not called");
+  if (e->precision != VXG_FP64) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: the FP64 precision is differentiated");
+  if (e->adj_scope) return fail(e, VXG_E_STATE, e->adj_scope);
+  if (e->g.collisions) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: collisions are outside the differentiated scope");
+  if (e->g.any_poisson) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: Poisson's ratio must be 0");
+  if (e->act_mode == 2 && e->n_phase < e->nv) return fail(e, VXG_E_STATE, "actuation phases cover fewer voxels than the scene");
+  for (int b = 0; b < n_bodies; ++b)
+    if (body_offsets[b] < 0 || body_offsets[b + 1] < body_offsets[b] || body_offsets[b + 1] > e->nv)
+      return fail(e, VXG_E_ARG, "vxg_adjoint_com_x: body offsets out of range");
+  VXG_CK(cudaSetDevice(e->device));
+  const int nv = e->nv, nl = e->nl, K = std::min(checkpoint_every, nsteps);
+  const int nck = (nsteps + K - 1) / K;
+  const size_t ckb = e->arena_bytes + sizeof(Ctl);
+  // one allocation for everything: checkpoints, final state, tape, adjoints
+  size_t off_ck = 0, sz = (size_t)(nck + 1) * ckb;
+  auto carve = [&](size_t bytes) { size_t o = (sz + 255) & ~(size_t)255; sz = o + bytes; return o; };
+  size_t o_tv = carve(sizeof(double) * 13 * (size_t)nv * K), o_tvf = carve(sizeof(uint32_t) * (size_t)nv * K),
+         o_tpd = carve(sizeof(float) * (size_t)nv * K), o_tl = carve(sizeof(double) * 9 * (size_t)nl * K),
+         o_tlf = carve(sizeof(uint32_t) * (size_t)nl * K), o_tt = carve(sizeof(float) * K),
+         o_lam = carve(sizeof(double) * 13 * (size_t)nv), o_gfm = carve(sizeof(double) * 6 * (size_t)nv),
+         o_mu = carve(sizeof(double) * 9 * (size_t)nl), o_lcon = carve(sizeof(double) * 14 * (size_t)nl),
+         o_lpar = carve(sizeof(double) * 4 * (size_t)nl), o_lf = carve(sizeof(double) * 12 * (size_t)nl),
+         o_gt = carve(sizeof(double) * nv), o_acc = carve(sizeof(double) * 3 * (size_t)nv),
+         o_err = carve(sizeof(int)), o_off = carve(sizeof(int) * ((size_t)n_bodies + 1)),
+         o_obj = carve(sizeof(double) * n_bodies);
+  char* buf = nullptr;
+  VXG_CK(cudaMalloc(&buf, sz));
+  struct Free { char* p; ~Free() { if (p) cudaFree(p); } } guard{buf};
+  AdjBuf T;
+  T.K = K;
+  T.tv = (double*)(buf + o_tv); T.tvf = (uint32_t*)(buf + o_tvf); T.tpd = (float*)(buf + o_tpd);
+  T.tl = (double*)(buf + o_tl); T.tlf = (uint32_t*)(buf + o_tlf); T.ttime = (float*)(buf + o_tt);
+  T.lam = (double*)(buf + o_lam); T.gFM = (double*)(buf + o_gfm); T.mu = (double*)(buf + o_mu);
+  T.lcon = (double*)(buf + o_lcon); T.lpar = (double*)(buf + o_lpar); T.lforce = (double*)(buf + o_lf);
+  T.gTempV = (double*)(buf + o_gt);
+  T.accE = (double*)(buf + o_acc); T.accRho = T.accE + nv; T.accPhase = T.accE + 2 * (size_t)nv;
+  T.err = (int*)(buf + o_err);
+  int* d_off = (int*)(buf + o_off);
+  double* d_obj = (double*)(buf + o_obj);
+  ActParams A{e->act_mode, e->act_amp, e->act_freq, e->act_mode == 2 ? e->d_phase : nullptr};
+  auto ck = [&](int c) { return buf + off_ck + (size_t)c * ckb; };
+  auto save = [&](int c) -> int {
+    VXG_CK(cudaMemcpyAsync(ck(c), e->arena, e->arena_bytes, cudaMemcpyDeviceToDevice, e->stream));
+    VXG_CK(cudaMemcpyAsync(ck(c) + e->arena_bytes, e->ctl, sizeof(Ctl), cudaMemcpyDeviceToDevice, e->stream));
+    return VXG_OK;
+  };
+  auto load = [&](int c) -> int {
+    VXG_CK(cudaMemcpyAsync(e->arena, ck(c), e->arena_bytes, cudaMemcpyDeviceToDevice, e->stream));
+    VXG_CK(cudaMemcpyAsync(e->ctl, ck(c) + e->arena_bytes, sizeof(Ctl), cudaMemcpyDeviceToDevice, e->stream));
+    return VXG_OK;
+  };
+  int rc;
+  // forward sweep, keeping the state at the start of every segment
+  for (int c = 0; c < nck; ++c) {
+    if ((rc = save(c))) return rc;
+    int n = std::min(K, nsteps - c * K), done = 0, div = 0;
+    if ((rc = vxg_step(e, n, dt, &done, &div))) return rc;
+    if (done != n || div) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: the forward run diverged");
+  }
+  if ((rc = save(nck))) return rc;
+  VXG_CK(cudaMemsetAsync(T.lam, 0, sizeof(double) * 13 * (size_t)nv, e->stream));
+  VXG_CK(cudaMemsetAsync(T.mu, 0, sizeof(double) * 9 * (size_t)nl, e->stream));
+  VXG_CK(cudaMemsetAsync(T.accE, 0, sizeof(double) * 3 * (size_t)nv, e->stream));
+  VXG_CK(cudaMemsetAsync(T.err, 0, sizeof(int), e->stream));
+  VXG_CK(cudaMemcpyAsync(d_off, body_offsets, sizeof(int) * ((size_t)n_bodies + 1), cudaMemcpyHostToDevice, e->stream));
+  k_adj_objective<<<n_bodies, 128, 0, e->stream>>>(e->S, T, d_off, d_obj);  // vxg_body_com's summation order
+  VXG_CK(cudaGetLastError());
+  const int gvx = grid_for(nv), glk = grid_for(std::max(nl, 1)), gboth = grid_for(std::max(nv, nl));
+  // reverse sweep: per segment, re-run it from its checkpoint recording the tape, then walk back
+  for (int c = nck - 1; c >= 0; --c) {
+    if ((rc = load(c))) return rc;
+    int n = std::min(K, nsteps - c * K);
+    for (int s = 0; s < n; ++s) {
+      k_tape_save<<<gboth, kBlock, 0, e->stream>>>(e->S, T, s);
+      enqueue_step(e, dt, s & 1);
+    }
+    for (int s = n - 1; s >= 0; --s) {
+      if (nl) k_adj_link_forces<<<glk, kBlock, 0, e->stream>>>(e->S, T, A, s);
+      k_adj_voxel<<<gvx, kBlock, 0, e->stream>>>(e->S, T, A, s, dt);
+      if (nl) k_adj_link<<<glk, kBlock, 0, e->stream>>>(e->S, T, A, s);
+      k_adj_gather<<<gvx, kBlock, 0, e->stream>>>(e->S, T, A, s);
+    }
+    VXG_CK(cudaGetLastError());
+  }
+  if ((rc = load(nck))) return rc;
+  int err = 0;
+  VXG_CK(cudaMemcpyAsync(&err, T.err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaMemcpyAsync(objective, d_obj, sizeof(double) * n_bodies, cudaMemcpyDeviceToHost, e->stream));
+  if (dE) VXG_CK(cudaMemcpyAsync(dE, T.accE, sizeof(double) * nv, cudaMemcpyDeviceToHost, e->stream));
+  if (drho) VXG_CK(cudaMemcpyAsync(drho, T.accRho, sizeof(double) * nv, cudaMemcpyDeviceToHost, e->stream));
+  if (dphase) VXG_CK(cudaMemcpyAsync(dphase, T.accPhase, sizeof(double) * nv, cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  VXG_CK(cudaGetLastError());
+  if (err & 1) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: a link left the small-angle branch (outside the differentiated scope)");
   return VXG_OK;
 }
 

@@ -252,6 +252,7 @@ _EXT_SIGS = {
     "restore": (_i, [_p, _i]),
     "set_launch": (_i, [_p, _i, _i, _i]),
     "autotune": (_i, [_p, _i, _f, _ip]),
+    "adjoint_com_x": (_i, [_p, _i, _f, _i, _ip, _i, _dp, _dp, _dp, _dp]),
 }
 
 ACT_OFF, ACT_UNIFORM, ACT_PER_VOXEL = 0, 1, 2
@@ -302,6 +303,18 @@ class Engine:
         out = np.zeros(3, np.int32)
         self._ck(self.f["autotune"](self.sim.h, trial_steps, dt, _ptr(out, C.c_int)))
         return tuple(int(x) for x in out)
+
+    def adjoint_com_x(self, nsteps: int, dt: float, body_offsets, checkpoint_every: int = 100):
+        """Run nsteps from the current state; return (per-body centre-of-mass x after the run,
+        dJ/dE, dJ/drho, dJ/dphase per voxel) for J = the sum of the per-body values."""
+        off = np.ascontiguousarray(body_offsets, np.int32)
+        nb, nv = len(off) - 1, self.sim.voxel_count()
+        obj = np.zeros(nb, np.float64)
+        gE, gR, gP = (np.zeros(nv, np.float64) for _ in range(3))
+        self._ck(self.f["adjoint_com_x"](self.sim.h, nsteps, dt, checkpoint_every, _ptr(off, C.c_int), nb,
+                                         _ptr(obj, C.c_double), _ptr(gE, C.c_double), _ptr(gR, C.c_double),
+                                         _ptr(gP, C.c_double)))
+        return obj, gE, gR, gP
 
     def read_positions(self) -> np.ndarray:
         n = self.sim.voxel_count()

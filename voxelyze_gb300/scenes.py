@@ -175,3 +175,30 @@ def population(n_bodies=4096, side_lo=4, side_hi=24, occupancy=0.6, seed=4, voxe
         body.append(np.full(len(xyz), b, np.int32))
     return Scene(voxel_size, [passive, active], np.concatenate(mats), np.concatenate(xyzs),
                  gravity=1.0, floor=True, body=np.concatenate(body), name=f"population_{n_bodies}")
+
+
+def graded_population(n_bodies=256, side=16, occupancy=0.7, seed=5, voxel_size=0.01, gap=2,
+                      E_range=(3e5, 3e6)) -> Scene:
+    """Bodies of side^3 cells (occupancy, largest component kept) on a 2-D grid, one material per
+    voxel with Young's modulus log-uniform in E_range, density 1000, CTE 0.01, friction 1.0/0.5;
+    floor and gravity.  ``phase`` (per-voxel actuation phase, uniform in [0, 2 pi)) is attached to
+    the returned scene."""
+    rng = np.random.default_rng(seed)
+    cols = int(np.ceil(np.sqrt(n_bodies)))
+    pitch = side + gap
+    xyzs, body = [], []
+    for b in range(n_bodies):
+        occ = largest_component(rng.random((side, side, side)) < occupancy)
+        ox, oy = (b % cols) * pitch, (b // cols) * pitch
+        xyz = _ordered(occ, offset=(ox, oy, 0))
+        xyzs.append(xyz)
+        body.append(np.full(len(xyz), b, np.int32))
+    xyz = np.concatenate(xyzs)
+    n = len(xyz)
+    lo, hi = np.log10(E_range[0]), np.log10(E_range[1])
+    E = (10.0 ** rng.uniform(lo, hi, n)).astype(np.float32)
+    mats = [Material(E=float(e), rho=1e3, cte=0.01, mu_static=1.0, mu_kinetic=0.5) for e in E]
+    sc = Scene(voxel_size, mats, np.arange(n, dtype=np.int32), xyz, gravity=1.0, floor=True,
+               body=np.concatenate(body), name=f"graded_population_{n_bodies}x{side}")
+    sc.phase = rng.uniform(0.0, 2.0 * np.pi, n).astype(np.float32)
+    return sc
