@@ -182,8 +182,16 @@ int vxg_body_com(vxg_engine* e, const int* offsets, int n_bodies, double* out);
  * the number of steps per captured CUDA graph replayed for long runs (even; 0 keeps). */
 int vxg_set_launch(vxg_engine* e, int block_link, int block_voxel, int graph_chunk);
 int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_chunk);
-/* Times short runs of the current scene for every block-size pair and several graph lengths and
- * keeps the fastest; the state is restored afterwards. */
+/* FP32C link pass (CVX_Link::updateForces, src/VX_Link.cpp:149-217) at a fixed dt: blocks_per_sm
+ * > 0 runs the pipelined kernel (a resident grid of that many blocks per SM, clamped to what fits;
+ * each tile's link state and endpoint gathers are copied into shared memory while the previous
+ * tile is computed), -1 as many blocks as fit, 0 (the default) the one-thread-per-link kernel.
+ * Both give identical results. */
+int vxg_set_link_pipeline(vxg_engine* e, int blocks_per_sm);
+int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm);
+/* Times short runs of the current scene for every block-size pair, (FP32C at a fixed dt) the
+ * pipelined link pass at several residencies, and several graph lengths, and keeps the fastest
+ * (the link-pass choice is read back with vxg_get_link_pipeline); the state is restored afterwards. */
 int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* best_voxel, int* best_chunk);
 /* Differentiated run of the FP64 path (no counterpart in the reference).  Runs nsteps steps of
  * length dt from the current state (the engine ends in the same state as after vxg_step) and

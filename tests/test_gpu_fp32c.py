@@ -111,3 +111,38 @@ def test_fp32c_state_roundtrip_and_reset(product_lib):
     assert np.array_equal(st_a["pos"], st_b["pos"])
     assert b.do_time_steps(50, dt) == 50
     assert np.all(np.isfinite(b.voxel_state()["pos"]))
+
+
+def _fp32c(product_lib, scene, blocks_per_sm):
+    s = make_sim(product_lib, "vx", scene)
+    E = F.Engine(s)
+    E.set_precision(1)
+    E.set_link_pipeline(blocks_per_sm)
+    assert E.link_pipeline() == blocks_per_sm
+    return s
+
+
+@pytest.mark.parametrize("scene", ["lattice_poisson", "cantilever", "population_actuated", "graded"])
+@pytest.mark.parametrize("blocks_per_sm", [-1, 1])
+def test_pipelined_link_pass_is_bit_identical(product_lib, scene, blocks_per_sm):
+    """The pipelined FP32C link pass (cp.async staging, resident grid) against the one-thread-per-
+    link pass: every state array identical bit for bit after each batch.  One block per SM makes
+    every block walk many tiles (both halves of the double buffer); the scenes cover Poisson's
+    ratio != 0 with bilinear materials, a fixed cantilever, in-step CTE actuation with floor and
+    friction, and one material per voxel."""
+    from conftest import state_diff
+
+    sc = {"lattice_poisson": lambda: S.lattice(40, 36, 20),
+          "cantilever": lambda: S.cantilever(40, 8, 8),
+          "population_actuated": lambda: S.population(24, 4, 12),
+          "graded": lambda: S.graded_population(6, 10)}[scene]()
+    a = _fp32c(product_lib, sc, 0)
+    b = _fp32c(product_lib, sc, blocks_per_sm)
+    dt = a.recommended_time_step()
+    assert b.recommended_time_step() == dt
+    if scene in ("population_actuated", "graded"):
+        for s in (a, b):
+            F.Engine(s).set_actuation(F.ACT_UNIFORM, 0.1, 2.0)
+    for _ in range(3):
+        assert a.do_time_steps(70, dt) == b.do_time_steps(70, dt) == 70
+        assert state_diff(a, b) == []

@@ -1393,6 +1393,16 @@ int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk) {
   if (!vx.upload()) return -1;
   return vxg_set_launch(vx.impl()->eng, block_link, block_voxel, graph_chunk) ? -1 : 0;
 }
+int vx_set_link_pipeline(void* s, int blocks_per_sm) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_set_link_pipeline(vx.impl()->eng, blocks_per_sm) ? -1 : 0;
+}
+int vx_get_link_pipeline(void* s, int* blocks_per_sm) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_get_link_pipeline(vx.impl()->eng, blocks_per_sm) ? -1 : 0;
+}
 int vx_autotune(void* s, int trial_steps, float dt, int* out3) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.upload() || !out3) return -1;

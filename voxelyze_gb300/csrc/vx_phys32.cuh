@@ -34,9 +34,9 @@ VX_HD q4 Q4(float w, float x, float y, float z) { q4 q; q.w = w; q.x = x; q.y = 
 // materials, externals, control block) is the FP64 View's.
 struct View {
   vx64::View B;     // shared arrays
-  float* d;         // 3 nv displacement from the lattice origin
-  float* c;         // 3 nv Kahan compensation (true displacement = d - c)
-  float* q;         // 4 nv orientation
+  float4* P;        // nv records (d.x, d.y, d.z, 0): displacement d from the lattice origin
+  float4* Q;        // nv records (w, x, y, z): orientation
+  float* c;         // 3 nv Kahan compensation of d (true displacement = d - c)
   float* qc;        // 4 nv Kahan compensation of the orientation (true orientation = q - qc)
   float* lin;       // 3 nv linear momentum
   float* ang;       // 3 nv angular momentum
@@ -187,24 +187,97 @@ VX_HD float link_freq2(const View& S, int l, int vn, int vp, int axis, const vxg
   return k / (m1 < m2 ? m1 : m2);
 }
 
-VX_HDN void link_update(const View& S, int l) {
+// Everything the link pass reads for one link, gathered before any arithmetic: the link's own
+// state, its endpoints' poses and materials and, where a material has Poisson's ratio != 0, their
+// cached Poisson strains.  The one-thread-per-link kernel fills it straight from global memory;
+// the pipelined kernel fills it from shared memory that cp.async staged one tile ahead.  Both then
+// run link_compute, so their results are identical bit for bit.
+struct LinkIn {
+  uint32_t lf;           // link flags (axis, small angle, local velocity valid)
+  int lmat;              // link material
+  float rd;              // rest length - nominal size
+  f3 oldPos2, oldA1, oldA2;
+  float tArea, tSS, maxStrain, strainOffset;
+  f3 dn, dp;             // endpoint displacements
+  q4 qn, qp;             // endpoint orientations
+  int vmn, vmp;          // endpoint voxel materials
+  f3 psn, psp;           // endpoint Poisson strains (read only for materials with nu != 0)
+};
+
+VX_HD f3 f3_of(const float4& a) { return F3(a.x, a.y, a.z); }
+VX_HD q4 q4_of(const float4& a) { return Q4(a.x, a.y, a.z, a.w); }
+
+// CVX_Voxel::transverseArea / transverseStrainSum from a voxel's material and Poisson strain
+VX_HD float transverse_area_of(const vxg_voxel_material& m, const f3& ps, int axis) {
+  float size = m.nomSizeF;
+  if (m.nu == 0) return size * size;
+  switch (axis) {
+    case 0: return size * size * (1 + ps.y) * (1 + ps.z);
+    case 1: return size * size * (1 + ps.x) * (1 + ps.z);
+    default: return size * size * (1 + ps.x) * (1 + ps.y);
+  }
+}
+VX_HD float transverse_strain_sum_of(const vxg_voxel_material& m, const f3& ps, int axis) {
+  if (m.nu == 0) return 0;
+  switch (axis) {
+    case 0: return ps.y + ps.z;
+    case 1: return ps.x + ps.z;
+    default: return ps.x + ps.y;
+  }
+}
+
+// POIS: some voxel material has nu != 0 (otherwise no Poisson strain is ever read)
+template <bool POIS>
+VX_HD LinkIn link_gather(const View& S, int l) {
   const vx64::View& B = S.B;
   const int nl = B.nl, nv = B.nv;
-  uint32_t lf = B.lflags[l];
+  LinkIn in;
+  in.lf = B.lflags[l];
+  in.lmat = B.lmat[l];
+  in.rd = S.restDelta[l];
+  in.oldPos2 = ld3(S.pos2, nl, l);
+  in.oldA1 = ld3(S.a1v, nl, l);
+  in.oldA2 = ld3(S.a2v, nl, l);
+  in.tArea = B.tArea[l];
+  in.tSS = B.tSS[l];
+  in.maxStrain = B.maxStrain[l];
+  in.strainOffset = B.strainOffset[l];
+  int vn = B.lvox[l], vp = B.lvox[nl + l];
+  in.dn = f3_of(S.P[vn]);
+  in.dp = f3_of(S.P[vp]);
+  in.qn = q4_of(S.Q[vn]);
+  in.qp = q4_of(S.Q[vp]);
+  in.vmn = B.vmat[vn];
+  in.vmp = B.vmat[vp];
+  if (POIS) {
+    in.psn = ld3(B.pStrain, nv, vn);
+    in.psp = ld3(B.pStrain, nv, vp);
+  } else {
+    in.psn = in.psp = F3(0, 0, 0);
+  }
+  return in;
+}
+
+// CVX_Link::updateForces + orientLink + updateStrain in FP32C for link l from its gathered inputs;
+// writes the link's new state and returns the axial strain (the divergence test's value).
+// pdt is every voxel's previous time step (the local damping divides by it).
+VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
+  const vx64::View& B = S.B;
+  const int nl = B.nl;
+  uint32_t lf = in.lf;
   int axis = (lf >> 8) & 3;
   bool smallAngle = lf & VXG_LF_SMALL_ANGLE;
   bool lvv = lf & VXG_LF_LOCAL_VEL_VALID;
-  int vn = B.lvox[l], vp = B.lvox[nl + l];
-  const vxg_link_material& m = B.lm[B.lmat[l]];
+  const vxg_link_material& m = B.lm[in.lmat];
   const float s = S.s;
-  float rd = S.restDelta[l];
+  float rd = in.rd;
   float L = s + rd;
 
-  f3 oldPos2 = ld3(S.pos2, nl, l), oldA1 = ld3(S.a1v, nl, l), oldA2 = ld3(S.a2v, nl, l);
-  f3 dn = ld3(S.d, nv, vn), dp = ld3(S.d, nv, vp);
+  const f3 oldPos2 = in.oldPos2, oldA1 = in.oldA1, oldA2 = in.oldA2;
+  const f3 dn = in.dn, dp = in.dp;
   f3 del = to_axis_x(axis, F3(dp.x - dn.x, dp.y - dn.y, dp.z - dn.z));
-  q4 a1 = to_axis_x(axis, ldq(S.q, nv, vn));
-  q4 a2 = to_axis_x(axis, ldq(S.q, nv, vp));
+  q4 a1 = to_axis_x(axis, in.qn);
+  q4 a2 = to_axis_x(axis, in.qp);
   q4 tr = Q4(a1.w, -a1.x, -a1.y, -a1.z);
   f3 r = rotate(tr, del);
   // pos2 = s * R e_x + R del, R = rotation by tr; the x part is split off to avoid s - s
@@ -243,15 +316,17 @@ VX_HDN void link_update(const View& S, int l) {
   f3 dA1 = F3(0.5f * (a1v.x - oldA1.x), 0.5f * (a1v.y - oldA1.y), 0.5f * (a1v.z - oldA1.z));
   f3 dA2 = F3(0.5f * (a2v.x - oldA2.x), 0.5f * (a2v.y - oldA2.y), 0.5f * (a2v.z - oldA2.z));
 
-  float tArea = B.tArea[l], tSS = B.tSS[l];
+  float tArea = in.tArea, tSS = in.tSS;
+  const vxg_voxel_material& mn = B.vm[in.vmn];
+  const vxg_voxel_material& mp = B.vm[in.vmp];
   if (!(m.nu == 0.0f) || tSS != 0) {
-    tArea = 0.5f * (transverse_area32(B, vn, axis) + transverse_area32(B, vp, axis));
-    tSS = 0.5f * (vx64::transverse_strain_sum(B, vn, axis) + vx64::transverse_strain_sum(B, vp, axis));
+    tArea = 0.5f * (transverse_area_of(mn, in.psn, axis) + transverse_area_of(mp, in.psp, axis));
+    tSS = 0.5f * (transverse_strain_sum_of(mn, in.psn, axis) + transverse_strain_sum_of(mp, in.psp, axis));
     B.tArea[l] = tArea;
     B.tSS[l] = tSS;
   }
   float axial = pos2.x / L;
-  float maxStrain = B.maxStrain[l], strainOffset = B.strainOffset[l], stress;
+  float maxStrain = in.maxStrain, strainOffset = in.strainOffset, stress;
   if (m.linear) {
     if (axial > maxStrain) maxStrain = axial;
     stress = vx64::mat_stress(m, axial, tSS, false);
@@ -281,9 +356,6 @@ VX_HDN void link_update(const View& S, int l) {
     mP = F3(a2c * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z));
     if (lvv) {
       f3 pc = F3(m.sqA1 * dPos2.x, m.sqB1 * dPos2.y - m.sqB2xFMp * (dA1.z + dA2.z), m.sqB1 * dPos2.z + m.sqB2xFMp * (dA1.y + dA2.y));
-      const vxg_voxel_material& mn = B.vm[B.vmat[vn]];
-      const vxg_voxel_material& mp = B.vm[B.vmat[vp]];
-      float pdt = B.ctl->last_dt;  // every voxel stepped with the same dt last step
       float dmN = 2 * mn.sqrtMass * mn.zetaInternal / pdt, dmP = 2 * mp.sqrtMass * mp.zetaInternal / pdt;
       fN.x += dmN * pc.x; fN.y += dmN * pc.y; fN.z += dmN * pc.z;
       fP.x -= dmP * pc.x; fP.y -= dmP * pc.y; fP.z -= dmP * pc.z;
@@ -313,7 +385,14 @@ VX_HDN void link_update(const View& S, int l) {
   st3(S.mN, nl, l, mN);
   st3(S.mP, nl, l, mP);
   B.lflags[l] = (lf & ~3u) | (smallAngle ? VXG_LF_SMALL_ANGLE : 0u) | (lvv ? VXG_LF_LOCAL_VEL_VALID : 0u);
+  return axial;
 }
+
+template <bool POIS>
+VX_HDN float link_update(const View& S, int l) {
+  return link_compute(S, l, link_gather<POIS>(S, l), S.B.ctl->last_dt);  // every voxel stepped with last_dt
+}
+
 
 VX_HD void kahan_add(float& sum, float& comp, float x) {
   float y = x - comp;
@@ -330,17 +409,17 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   int ei = B.vext[v];
   const vxg_external* e = ei >= 0 ? &B.ext[ei] : nullptr;
   if (e && (e->dof & 0x3F) == 0x3F) {
-    st3(S.d, nv, v, F3((float)e->translation[0], (float)e->translation[1], (float)e->translation[2]));
+    S.P[v] = make_float4((float)e->translation[0], (float)e->translation[1], (float)e->translation[2], 0.0f);
     st3(S.c, nv, v, F3(0, 0, 0));
-    stq(S.q, nv, v, Q4((float)e->rotq[0], (float)e->rotq[1], (float)e->rotq[2], (float)e->rotq[3]));
+    S.Q[v] = make_float4((float)e->rotq[0], (float)e->rotq[1], (float)e->rotq[2], (float)e->rotq[3]);
     stq(S.qc, nv, v, Q4(0, 0, 0, 0));
     st3(S.lin, nv, v, F3(0, 0, 0));
     st3(S.ang, nv, v, F3(0, 0, 0));
     return;
   }
   uint32_t flags = B.vflags[v];
-  f3 d = ld3(S.d, nv, v), c = ld3(S.c, nv, v), lin = ld3(S.lin, nv, v), ang = ld3(S.ang, nv, v);
-  q4 q = ldq(S.q, nv, v), qc = ldq(S.qc, nv, v);
+  f3 d = f3_of(S.P[v]), c = ld3(S.c, nv, v), lin = ld3(S.lin, nv, v), ang = ld3(S.ang, nv, v);
+  q4 q = q4_of(S.Q[v]), qc = ldq(S.qc, nv, v);
   int lk[6];
 #pragma unroll
   for (int i = 0; i < 6; ++i) lk[i] = B.vlinks[i * nv + v];
@@ -449,11 +528,11 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
       }
     }
   }
-  st3(S.d, nv, v, d);
+  S.P[v] = make_float4(d.x, d.y, d.z, 0.0f);
   st3(S.c, nv, v, c);
   st3(S.lin, nv, v, lin);
   st3(S.ang, nv, v, ang);
-  stq(S.q, nv, v, q);
+  S.Q[v] = make_float4(q.w, q.x, q.y, q.z);
   stq(S.qc, nv, v, qc);
   B.vflags[v] = (flags & ~(uint32_t)VXG_VF_STATIC_FRICTION) | (staticF ? VXG_VF_STATIC_FRICTION : 0u) |
                 VXG_VF_PSTRAIN_INVALID;

@@ -251,7 +251,7 @@ int grid_for(int n) { return std::max(1, (n + kBlock - 1) / kBlock); }
 int grid_of(int n, int b) { return std::max(1, (n + b - 1) / b); }
 
 // ---- FP32C kernels ------------------------------------------------------------------------
-template <bool RECOMMEND, bool FORCES>
+template <bool RECOMMEND, bool FORCES, bool POIS>
 __global__ void __launch_bounds__(512) k_link32(vx32::View S, int parity) {
   int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (S.B.ctl->halt) return;
@@ -264,8 +264,145 @@ __global__ void __launch_bounds__(512) k_link32(vx32::View S, int parity) {
   }
   if (RECOMMEND) block_max_to(&S.B.ctl->maxf[parity], f2);
   if (!FORCES || !live) return;
-  vx32::link_update(S, l);
-  if (S.B.strain[l] > 100) S.B.ctl->diverged = 1;
+  if (vx32::link_update<POIS>(S, l) > 100) S.B.ctl->diverged = 1;
+}
+
+// ---- pipelined FP32C link pass ----------------------------------------------------------------
+// The one-thread-per-link pass is latency bound: each link's work waits on a chain of dependent
+// loads (link -> endpoint ids -> endpoint poses and materials), and the registers of its arithmetic
+// leave too few warps resident to cover that chain.  Here a resident grid walks tiles of kLpT
+// links (one link per thread, tiles handed out round robin); while a tile is computed, the next
+// tile's link state and endpoint gathers are already in flight as cp.async copies into the other
+// half of a double-buffered shared-memory stage, and the endpoint ids of the tile after that are
+// in flight as plain loads.  Each thread copies and later reads only its own link's slots, so no
+// block barrier is needed: cp.async.wait_group makes a thread's own copies visible to it.
+constexpr int kLpT = 128;                                 // links per tile = threads per block
+constexpr int kLpF4 = 4;                                  // float4 slots per link: P, Q of both ends
+constexpr int kLpW = 24;                                  // 4-byte slots per link
+constexpr int kLpStage = kLpT * (16 * kLpF4 + 4 * kLpW);  // bytes per stage (20 KB)
+constexpr int kLpSmem = 2 * kLpStage;
+// 4-byte slot indices
+enum { LW_FLAGS, LW_MAT, LW_RD, LW_POS2, LW_A1 = LW_POS2 + 3, LW_A2 = LW_A1 + 3, LW_TAREA = LW_A2 + 3, LW_TSS,
+       LW_MAXS, LW_SOFF, LW_VMN, LW_VMP, LW_PSN, LW_PSP = LW_PSN + 3, LW_END = LW_PSP + 3 };
+static_assert(LW_END == kLpW, "slot count");
+
+__device__ __forceinline__ void cp_async4(void* sdst, const void* gsrc) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// stage layout: float4 slots [kLpF4][kLpT], then 4-byte slots [kLpW][kLpT]
+template <bool POIS>
+__device__ __forceinline__ void lp_issue(const vx32::View& S, char* stage, int t, int l, int vn, int vp) {
+  const vx64::View& B = S.B;
+  const int nl = B.nl, nv = B.nv;
+  float4* f4 = reinterpret_cast<float4*>(stage);
+  uint32_t* w = reinterpret_cast<uint32_t*>(stage + 16 * kLpF4 * kLpT);
+  cp_async16(&f4[0 * kLpT + t], &S.P[vn]);
+  cp_async16(&f4[1 * kLpT + t], &S.Q[vn]);
+  cp_async16(&f4[2 * kLpT + t], &S.P[vp]);
+  cp_async16(&f4[3 * kLpT + t], &S.Q[vp]);
+  cp_async4(&w[LW_VMN * kLpT + t], &B.vmat[vn]);
+  cp_async4(&w[LW_VMP * kLpT + t], &B.vmat[vp]);
+  cp_async4(&w[LW_FLAGS * kLpT + t], &B.lflags[l]);
+  cp_async4(&w[LW_MAT * kLpT + t], &B.lmat[l]);
+  cp_async4(&w[LW_RD * kLpT + t], &S.restDelta[l]);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    cp_async4(&w[(LW_POS2 + k) * kLpT + t], &S.pos2[k * nl + l]);
+    cp_async4(&w[(LW_A1 + k) * kLpT + t], &S.a1v[k * nl + l]);
+    cp_async4(&w[(LW_A2 + k) * kLpT + t], &S.a2v[k * nl + l]);
+  }
+  cp_async4(&w[LW_TAREA * kLpT + t], &B.tArea[l]);
+  cp_async4(&w[LW_TSS * kLpT + t], &B.tSS[l]);
+  cp_async4(&w[LW_MAXS * kLpT + t], &B.maxStrain[l]);
+  cp_async4(&w[LW_SOFF * kLpT + t], &B.strainOffset[l]);
+  if (POIS) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      cp_async4(&w[(LW_PSN + k) * kLpT + t], &B.pStrain[k * nv + vn]);
+      cp_async4(&w[(LW_PSP + k) * kLpT + t], &B.pStrain[k * nv + vp]);
+    }
+  }
+}
+
+template <bool POIS>
+__device__ __forceinline__ vx32::LinkIn lp_read(const char* stage, int t) {
+  const float4* f4 = reinterpret_cast<const float4*>(stage);
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(stage + 16 * kLpF4 * kLpT);
+  auto F = [&](int k) { return __uint_as_float(w[k * kLpT + t]); };
+  vx32::LinkIn in;
+  in.dn = vx32::f3_of(f4[0 * kLpT + t]);
+  in.qn = vx32::q4_of(f4[1 * kLpT + t]);
+  in.dp = vx32::f3_of(f4[2 * kLpT + t]);
+  in.qp = vx32::q4_of(f4[3 * kLpT + t]);
+  in.vmn = (int)w[LW_VMN * kLpT + t];
+  in.vmp = (int)w[LW_VMP * kLpT + t];
+  in.lf = w[LW_FLAGS * kLpT + t];
+  in.lmat = (int)w[LW_MAT * kLpT + t];
+  in.rd = F(LW_RD);
+  in.oldPos2 = vx32::F3(F(LW_POS2), F(LW_POS2 + 1), F(LW_POS2 + 2));
+  in.oldA1 = vx32::F3(F(LW_A1), F(LW_A1 + 1), F(LW_A1 + 2));
+  in.oldA2 = vx32::F3(F(LW_A2), F(LW_A2 + 1), F(LW_A2 + 2));
+  in.tArea = F(LW_TAREA);
+  in.tSS = F(LW_TSS);
+  in.maxStrain = F(LW_MAXS);
+  in.strainOffset = F(LW_SOFF);
+  if (POIS) {
+    in.psn = vx32::F3(F(LW_PSN), F(LW_PSN + 1), F(LW_PSN + 2));
+    in.psp = vx32::F3(F(LW_PSP), F(LW_PSP + 1), F(LW_PSP + 2));
+  } else {
+    in.psn = in.psp = vx32::F3(0, 0, 0);
+  }
+  return in;
+}
+
+template <bool POIS>
+__global__ void __launch_bounds__(kLpT) k_link32p(vx32::View S, int ntiles) {
+  extern __shared__ __align__(16) char lp_smem[];
+  const vx64::View& B = S.B;
+  if (B.ctl->halt) return;
+  const int t = threadIdx.x, nl = B.nl, G = gridDim.x;
+  const float pdt = B.ctl->last_dt;  // every voxel stepped with the same dt last step
+  int tile = blockIdx.x;
+  if (tile >= ntiles) return;
+  // prologue: ids of the first two tiles, copies of the first
+  int l = tile * kLpT + t;
+  if (l < nl) lp_issue<POIS>(S, lp_smem, t, l, B.lvox[l], B.lvox[nl + l]);
+  cp_async_commit();
+  int nt = tile + G;
+  int l1 = nt * kLpT + t;
+  bool ok1 = nt < ntiles && l1 < nl;
+  int vn1 = 0, vp1 = 0;
+  if (ok1) { vn1 = B.lvox[l1]; vp1 = B.lvox[nl + l1]; }
+  bool diverged = false;
+  for (int k = 0; tile < ntiles; ++k) {
+    char* cur = lp_smem + (k & 1) * kLpStage;
+    char* nxt = lp_smem + ((k & 1) ^ 1) * kLpStage;
+    const int t2 = nt + G;
+    const int l2 = t2 * kLpT + t;
+    const bool ok2 = t2 < ntiles && l2 < nl;
+    int vn2 = 0, vp2 = 0;
+    if (ok2) { vn2 = B.lvox[l2]; vp2 = B.lvox[nl + l2]; }
+    if (ok1) lp_issue<POIS>(S, nxt, t, l1, vn1, vp1);
+    cp_async_commit();
+    cp_async_wait1();  // this tile's copies (all but the group just committed) have landed
+    l = tile * kLpT + t;
+    if (l < nl) diverged |= vx32::link_compute(S, l, lp_read<POIS>(cur, t), pdt) > 100;
+    tile = nt;
+    nt = t2;
+    l1 = l2;
+    ok1 = ok2;
+    vn1 = vn2;
+    vp1 = vp2;
+  }
+  if (diverged) B.ctl->diverged = 1;
 }
 
 template <bool RECOMMEND>
@@ -306,10 +443,11 @@ __global__ void k_conv(vx32::View S, double s, int field, int to32) {
           if (to32) {
             double dd = B.pos[k * nv + i] - B.vidx[k * nv + i] * s;
             float d = (float)dd;
-            S.d[k * nv + i] = d;
+            reinterpret_cast<float*>(&S.P[i])[k] = d;
             S.c[k * nv + i] = (float)((double)d - dd);  // true displacement = d - c
           } else {
-            B.pos[k * nv + i] = B.vidx[k * nv + i] * s + ((double)S.d[k * nv + i] - (double)S.c[k * nv + i]);
+            B.pos[k * nv + i] = B.vidx[k * nv + i] * s +
+                                ((double)reinterpret_cast<const float*>(&S.P[i])[k] - (double)S.c[k * nv + i]);
           }
         }
       break;
@@ -320,10 +458,10 @@ __global__ void k_conv(vx32::View S, double s, int field, int to32) {
           if (to32) {
             double q64 = B.orient[k * nv + i];
             float q = (float)q64;
-            S.q[k * nv + i] = q;
+            reinterpret_cast<float*>(&S.Q[i])[k] = q;
             S.qc[k * nv + i] = (float)((double)q - q64);  // true orientation = q - qc
           } else {
-            B.orient[k * nv + i] = (double)S.q[k * nv + i] - (double)S.qc[k * nv + i];
+            B.orient[k * nv + i] = (double)reinterpret_cast<const float*>(&S.Q[i])[k] - (double)S.qc[k * nv + i];
           }
         }
       break;
@@ -370,16 +508,17 @@ __global__ void k_actuate(View S, double amp, double freq, const float* phase, i
 }
 
 // mass-weighted centre of mass of contiguous voxel ranges (one block per body), double accumulation
-__global__ void k_body_com(View S, const float* d32, const float* c32, double s, const int* off, double* out) {
+__global__ void k_body_com(View S, const float4* d32, const float* c32, double s, const int* off, double* out) {
   int b = blockIdx.x;
   int lo = off[b], hi = off[b + 1];
   double m = 0, x = 0, y = 0, z = 0;
   for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
     double mv = S.vm[S.vmat[v]].mass, px, py, pz;
     if (d32) {
-      px = S.vidx[v] * s + ((double)d32[v] - (double)c32[v]);
-      py = S.vidx[S.nv + v] * s + ((double)d32[S.nv + v] - (double)c32[S.nv + v]);
-      pz = S.vidx[2 * S.nv + v] * s + ((double)d32[2 * S.nv + v] - (double)c32[2 * S.nv + v]);
+      float4 d = d32[v];
+      px = S.vidx[v] * s + ((double)d.x - (double)c32[v]);
+      py = S.vidx[S.nv + v] * s + ((double)d.y - (double)c32[S.nv + v]);
+      pz = S.vidx[2 * S.nv + v] * s + ((double)d.z - (double)c32[2 * S.nv + v]);
     } else {
       px = S.pos[v]; py = S.pos[S.nv + v]; pz = S.pos[2 * S.nv + v];
     }
@@ -493,6 +632,12 @@ struct vxg_engine {
   int graph_chunk = 64;
   // launch shapes (vxg_set_launch / vxg_autotune)
   int blk_link = 256, blk_voxel = 256;
+  // FP32C link pass: resident blocks per SM of the pipelined kernel (-1: as many as fit; 0, the
+  // default: the one-thread-per-link kernel instead), and the occupancy limits found for it
+  int lp_bps = 0;
+  int lp_fit[2] = {0, 0};
+  int n_sm = 0;
+  bool tab_poisson = false;  // some voxel material has nu != 0
   // per-step actuation (vxg_set_actuation)
   int act_mode = 0;
   double act_amp = 0, act_freq = 0;
@@ -769,14 +914,15 @@ int vxg_resize(vxg_engine* e, int nv, int nl) {
   e->arena_bytes = total;
   for (int f = 0; f < VXG_F_TIME; ++f) e->field_ptr[f] = e->arena + off[f];
   if (e->precision == VXG_FP32C) {
-    size_t vb = ((sizeof(float) * 20 * (size_t)nv + 255) / 256) * 256;
+    size_t vb = ((sizeof(float) * 21 * (size_t)nv + 255) / 256) * 256;
     size_t lb = ((sizeof(float) * 22 * (size_t)nl + 255) / 256) * 256;
     e->arena32_bytes = std::max<size_t>(vb + lb, 256);
     VXG_CK(cudaMalloc(&e->arena32, e->arena32_bytes));
     VXG_CK(cudaMemsetAsync(e->arena32, 0, vb + lb, e->stream));
     float* p = (float*)e->arena32;
-    e->V.d = p; e->V.c = p + 3 * (size_t)nv; e->V.q = p + 6 * (size_t)nv;
-    e->V.lin = p + 10 * (size_t)nv; e->V.ang = p + 13 * (size_t)nv; e->V.qc = p + 16 * (size_t)nv;
+    // float4 records first (16-byte aligned), then the per-component arrays
+    e->V.P = (float4*)p; e->V.Q = (float4*)(p + 4 * (size_t)nv); e->V.c = p + 8 * (size_t)nv;
+    e->V.qc = p + 11 * (size_t)nv; e->V.lin = p + 15 * (size_t)nv; e->V.ang = p + 18 * (size_t)nv;
     float* L = (float*)(e->arena32 + vb);
     e->V.pos2 = L; e->V.a1v = L + 3 * (size_t)nl; e->V.a2v = L + 6 * (size_t)nl; e->V.fN = L + 9 * (size_t)nl;
     e->V.fP = L + 12 * (size_t)nl; e->V.mN = L + 15 * (size_t)nl; e->V.mP = L + 18 * (size_t)nl;
@@ -839,6 +985,9 @@ int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const 
   if ((rc = upload_table(e, &e->d_vm, &e->n_vm, vm, n_vm))) return rc;
   if ((rc = upload_table(e, &e->d_lm, &e->n_lm, lm, n_lm))) return rc;
   if ((rc = upload_table(e, &e->d_ext, &e->n_ext, ext, n_ext))) return rc;
+  e->tab_poisson = false;
+  for (int k = 0; k < n_vm; ++k)
+    if (vm[k].nu != 0.0f) e->tab_poisson = true;
   e->adj_scope = nullptr;
   for (int k = 0; k < n_lm && !e->adj_scope; ++k)
     if (!lm[k].linear || lm[k].nu != 0.0f || lm[k].epsilonFail != -1.0f)
@@ -894,6 +1043,20 @@ int vxg_set_nearby(vxg_engine* e, const int* offsets, const int* items, long lon
   return VXG_OK;
 }
 
+// blocks of the pipelined link kernel resident on the whole GPU (occupancy queried once)
+static int lp_resident(vxg_engine* e, bool pois) {
+  int& fit = e->lp_fit[pois ? 1 : 0];
+  if (!fit) {
+    if (!e->n_sm) cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->device);
+    int nb = 0;
+    if (pois) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_link32p<true>, kLpT, kLpSmem);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_link32p<false>, kLpT, kLpSmem);
+    fit = std::max(1, nb);
+  }
+  int bps = e->lp_bps > 0 ? std::min(e->lp_bps, fit) : fit;
+  return std::max(1, e->n_sm) * bps;
+}
+
 // enqueue one step (no synchronisation); in timing mode `ev` holds this step's 4 events
 static void enqueue_step(vxg_engine* e, float dt, int parity, cudaEvent_t* ev = nullptr) {
   const View& S = e->S;
@@ -912,8 +1075,19 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, cudaEvent_t* ev = 
   if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S);
   if (e->precision == VXG_FP32C) {
     if (e->nl) {
-      if (rec) k_link32<true, true><<<gl, bl, 0, e->stream>>>(e->V, parity);
-      else k_link32<false, true><<<gl, bl, 0, e->stream>>>(e->V, parity);
+      const bool pois = e->tab_poisson;
+      if (rec) {
+        if (pois) k_link32<true, true, true><<<gl, bl, 0, e->stream>>>(e->V, parity);
+        else k_link32<true, true, false><<<gl, bl, 0, e->stream>>>(e->V, parity);
+      } else if (e->lp_bps != 0) {
+        const int ntiles = (e->nl + kLpT - 1) / kLpT;
+        const int grid = std::min(ntiles, lp_resident(e, pois));
+        if (pois) k_link32p<true><<<grid, kLpT, kLpSmem, e->stream>>>(e->V, ntiles);
+        else k_link32p<false><<<grid, kLpT, kLpSmem, e->stream>>>(e->V, ntiles);
+      } else {
+        if (pois) k_link32<false, true, true><<<gl, bl, 0, e->stream>>>(e->V, parity);
+        else k_link32<false, true, false><<<gl, bl, 0, e->stream>>>(e->V, parity);
+      }
     }
     if (ev) cudaEventRecord(ev[1], e->stream);
     if (ev) cudaEventRecord(ev[2], e->stream);
@@ -1150,7 +1324,7 @@ int vxg_recommended_dt(vxg_engine* e, float* dt) {
   ensure32(e);
   if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S);
   if (e->precision == VXG_FP32C) {
-    if (e->nl) k_link32<true, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, 0);
+    if (e->nl) k_link32<true, false, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, 0);
     e->stale64 |= 1u << VXG_F_REST_LENGTH;
   } else if (e->nl) {
     k_link<true, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S, 0);
@@ -1260,7 +1434,7 @@ int vxg_body_com(vxg_engine* e, const int* offsets, int n_bodies, double* out) {
   ensure32(e);
   VXG_CK(cudaMemcpyAsync(e->d_body_off, offsets, sizeof(int) * ((size_t)n_bodies + 1), cudaMemcpyHostToDevice, e->stream));
   bool fp32 = e->precision == VXG_FP32C;
-  k_body_com<<<n_bodies, 128, 0, e->stream>>>(e->S, fp32 ? e->V.d : nullptr, fp32 ? e->V.c : nullptr, e->g.voxSize,
+  k_body_com<<<n_bodies, 128, 0, e->stream>>>(e->S, fp32 ? e->V.P : nullptr, fp32 ? e->V.c : nullptr, e->g.voxSize,
                                              e->d_body_off, e->d_body_out);
   VXG_CK(cudaMemcpyAsync(out, e->d_body_out, sizeof(double) * 3 * (size_t)n_bodies, cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
@@ -1279,6 +1453,17 @@ int vxg_set_launch(vxg_engine* e, int block_link, int block_voxel, int graph_chu
   return VXG_OK;
 }
 
+int vxg_set_link_pipeline(vxg_engine* e, int blocks_per_sm) {
+  if (!e || blocks_per_sm < -1 || blocks_per_sm > 64) return VXG_E_ARG;
+  e->lp_bps = blocks_per_sm;
+  e->graph_valid = false;
+  return VXG_OK;
+}
+int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm) {
+  if (!e || !blocks_per_sm) return VXG_E_ARG;
+  *blocks_per_sm = e->lp_bps;
+  return VXG_OK;
+}
 int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_chunk) {
   if (!e) return VXG_E_ARG;
   if (block_link) *block_link = e->blk_link;
@@ -1341,10 +1526,12 @@ int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* 
   if (rc) return rc;
   const int cand[4] = {64, 128, 256, 512};
   float best = 1e30f;
-  int bl = e->blk_link, bv = e->blk_voxel, bc = e->graph_chunk;
+  int bl = e->blk_link, bv = e->blk_voxel, bc = e->graph_chunk, bps = e->lp_bps;
   int timing = e->timing;
   e->timing = 1;
-  for (int a = 0; a < 4; ++a)
+  float t_link_best = 1e30f;  // the best one-thread-per-link pass, against the pipelined one below
+  e->lp_bps = 0;
+  for (int a = 0; a < 4 && !rc; ++a)
     for (int b = 0; b < 4; ++b) {
       e->blk_link = cand[a];
       e->blk_voxel = cand[b];
@@ -1353,13 +1540,30 @@ int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* 
       if ((rc = vxg_restore(e, slot))) break;
       if (e->t_link + e->t_vox < best) {
         best = e->t_link + e->t_vox;
+        t_link_best = e->t_link;
         bl = cand[a];
         bv = cand[b];
       }
     }
-  e->timing = timing;
   e->blk_link = bl;
   e->blk_voxel = bv;
+  bps = 0;
+  // FP32C at a fixed dt: the pipelined link pass at several residencies
+  if (!rc && e->precision == VXG_FP32C && dt > 0 && e->nl) {
+    const int res[4] = {-1, 2, 3, 4};
+    for (int a = 0; a < 4; ++a) {
+      e->lp_bps = res[a];
+      int done = 0, div = 0;
+      if ((rc = vxg_step(e, trial_steps, dt, &done, &div))) break;
+      if ((rc = vxg_restore(e, slot))) break;
+      if (e->t_link < t_link_best) {
+        t_link_best = e->t_link;
+        bps = res[a];
+      }
+    }
+  }
+  e->lp_bps = bps;
+  e->timing = timing;
   // graph chunk: replay throughput of a few candidate lengths
   if (!rc) {
     float bestc = 1e30f;

@@ -252,6 +252,8 @@ _EXT_SIGS = {
     "restore": (_i, [_p, _i]),
     "set_launch": (_i, [_p, _i, _i, _i]),
     "autotune": (_i, [_p, _i, _f, _ip]),
+    "set_link_pipeline": (_i, [_p, _i]),
+    "get_link_pipeline": (_i, [_p, _ip]),
     "adjoint_com_x": (_i, [_p, _i, _f, _i, _ip, _i, _dp, _dp, _dp, _dp]),
 }
 
@@ -298,6 +300,16 @@ class Engine:
 
     def set_launch(self, block_link: int = 0, block_voxel: int = 0, graph_chunk: int = 0):
         self._ck(self.f["set_launch"](self.sim.h, block_link, block_voxel, graph_chunk))
+
+    def set_link_pipeline(self, blocks_per_sm: int):
+        """FP32C link pass: >0 pipelined kernel with that many resident blocks per SM, -1 as many
+        as fit, 0 the one-thread-per-link kernel (default)."""
+        self._ck(self.f["set_link_pipeline"](self.sim.h, blocks_per_sm))
+
+    def link_pipeline(self) -> int:
+        out = np.zeros(1, np.int32)
+        self._ck(self.f["get_link_pipeline"](self.sim.h, _ptr(out, C.c_int)))
+        return int(out[0])
 
     def autotune(self, trial_steps: int = 20, dt: float = -1.0) -> tuple:
         out = np.zeros(3, np.int32)
