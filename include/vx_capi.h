@@ -85,6 +85,7 @@ int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk); /*
 int vx_autotune(void* s, int trial_steps, float dt, int* out3);            /* vxg_autotune: link, voxel, chunk */
 int vx_set_link_pipeline(void* s, int blocks_per_sm);                      /* vxg_set_link_pipeline */
 int vx_get_link_pipeline(void* s, int* blocks_per_sm);                     /* vxg_get_link_pipeline */
+int vx_set_poisson_fusion(void* s, int on);                                /* vxg_set_poisson_fusion */
 
 #ifdef __cplusplus
 }

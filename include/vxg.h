@@ -40,7 +40,12 @@ enum { VXG_OK = 0, VXG_E_ARG = -1, VXG_E_CUDA = -2, VXG_E_STATE = -3, VXG_E_SIZE
 
 /* voxel flag bits (per voxel, uint32) */
 enum { VXG_VF_FLOOR = 1, VXG_VF_STATIC_FRICTION = 2, VXG_VF_COLLISIONS = 4, VXG_VF_INTERIOR = 8,
-       VXG_VF_PSTRAIN_INVALID = 16 };
+       VXG_VF_PSTRAIN_INVALID = 16,
+       /* FP32C: the Poisson-strain cache was filled by the voxel pass from that step's link strains,
+        * ahead of the next link pass that the reference fills it in (src/VX_Voxel.cpp:336-343).  It
+        * equals the lazy value unless externals, materials or link state were edited since; after
+        * such an edit the next step recomputes it first. */
+       VXG_VF_PSTRAIN_EAGER = 32 };
 /* link flag bits (per link, uint32); bits 8..9 hold the axis */
 enum { VXG_LF_SMALL_ANGLE = 1, VXG_LF_LOCAL_VEL_VALID = 2 };
 
@@ -189,6 +194,12 @@ int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_
  * Both give identical results. */
 int vxg_set_link_pipeline(vxg_engine* e, int blocks_per_sm);
 int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm);
+/* FP32C with Poisson's ratio != 0: on (the default), the voxel pass fills each voxel's Poisson-
+ * strain cache for the next step's link pass from that step's link strains (CVX_Voxel::strain,
+ * src/VX_Voxel.cpp:300-343, which the reference evaluates lazily in the next link pass); off, a
+ * pre-pass fills it before every link pass.  Both give identical positions, momenta and link
+ * state; the cached values read between steps are the ones the next step will use. */
+int vxg_set_poisson_fusion(vxg_engine* e, int on);
 /* Times short runs of the current scene for every block-size pair, (FP32C at a fixed dt) the
  * pipelined link pass at several residencies, and several graph lengths, and keeps the fastest
  * (the link-pass choice is read back with vxg_get_link_pipeline); the state is restored afterwards. */

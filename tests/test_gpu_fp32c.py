@@ -146,3 +146,37 @@ def test_pipelined_link_pass_is_bit_identical(product_lib, scene, blocks_per_sm)
     for _ in range(3):
         assert a.do_time_steps(70, dt) == b.do_time_steps(70, dt) == 70
         assert state_diff(a, b) == []
+
+
+def _dynamic_state(s):
+    v, l = s.voxel_state(), s.link_state()
+    return [v["raw_d"], v["temp"], v["staticFriction"], l["raw_d"], l["raw_f"], l["raw_i"]]
+
+
+@pytest.mark.parametrize("edit", [False, True])
+def test_fused_poisson_cache_matches_prepass(product_lib, edit):
+    """FP32C with nu = 0.3: the voxel pass filling each Poisson-strain cache for the next step
+    (default) against a pre-pass filling it before every link pass.  Positions, momenta,
+    orientations, temperatures and every link-state array are identical bit for bit after each
+    batch.  With `edit`, between batches forces on the x-max face change (their x component decides
+    the tension terms of CVX_Voxel::strain, src/VX_Voxel.cpp:313-318) and the x = 0 face gets
+    fixed: the caches filled ahead of time must be refilled from the edited externals."""
+    sc = S.lattice(24, 20, 12)
+    a = _fp32c(product_lib, sc, 0)
+    b = _fp32c(product_lib, sc, 0)
+    F.Engine(b).set_poisson_fusion(False)
+    dt = a.recommended_time_step()
+    assert b.recommended_time_step() == dt
+    xmax = np.flatnonzero(sc.xyz[:, 0] == sc.xyz[:, 0].max())
+    x0 = np.flatnonzero(sc.xyz[:, 0] == 0)
+    for k in range(4):
+        if edit:
+            for s in (a, b):
+                for v in xmax:
+                    s.set_force(int(v), 0.02 * (k - 1), 0.0, -0.01 * k)
+                if k == 2:
+                    for v in x0:
+                        s.set_fixed_all(int(v))
+        assert a.do_time_steps(40, dt) == b.do_time_steps(40, dt) == 40
+        for x, y in zip(_dynamic_state(a), _dynamic_state(b)):
+            assert np.array_equal(x, y)

@@ -104,7 +104,10 @@ void CVoxelyze::clear() {  // Voxelyze.cpp:323-355
 void CVoxelyze::markState() const {
   pimpl->state_dirty = true;
 }
-void CVoxelyze::markTables() { pimpl->tables_dirty = true; }
+void CVoxelyze::markTables() {
+  pimpl->tables_dirty = true;
+  pimpl->eager_stale = true;
+}
 void CVoxelyze::markTopology() {
   pimpl->topo_dirty = true;
   pimpl->tables_dirty = true;
@@ -664,6 +667,7 @@ int CVoxelyze::doTimeSteps(int n, float dt) {
   int rc = vxg_step(pimpl->eng, n, dt, &done, &div);
   pimpl->device_ahead = true;
   if (rc) { pimpl->err = vxg_last_error(pimpl->eng); return -1; }
+  if (done > 0) pimpl->eager_stale = false;
   return done;
 }
 
@@ -982,10 +986,10 @@ Vec3D<float> CVX_Voxel::cornerPosition(voxelCorner corner) const {  // VX_Voxel.
 // (VX_Voxel.cpp:336-374), on the mirror
 Vec3D<float> CVX_Voxel::poissonsStrain() {
   VxImpl& I = *vx->pimpl;
-  if (I.vflags[idx] & VXG_VF_PSTRAIN_INVALID) {
+  if ((I.vflags[idx] & VXG_VF_PSTRAIN_INVALID) || ((I.vflags[idx] & VXG_VF_PSTRAIN_EAGER) && I.eager_stale)) {
     Vec3D<float> p = strain(true);
     I.vf[VF_PSX][idx] = p.x; I.vf[VF_PSY][idx] = p.y; I.vf[VF_PSZ][idx] = p.z;
-    I.vflags[idx] &= ~(uint32_t)VXG_VF_PSTRAIN_INVALID;
+    I.vflags[idx] &= ~(uint32_t)(VXG_VF_PSTRAIN_INVALID | VXG_VF_PSTRAIN_EAGER);
   }
   return Vec3D<float>(I.vf[VF_PSX][idx], I.vf[VF_PSY][idx], I.vf[VF_PSZ][idx]);
 }
@@ -1397,6 +1401,11 @@ int vx_set_link_pipeline(void* s, int blocks_per_sm) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.upload()) return -1;
   return vxg_set_link_pipeline(vx.impl()->eng, blocks_per_sm) ? -1 : 0;
+}
+int vx_set_poisson_fusion(void* s, int on) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_set_poisson_fusion(vx.impl()->eng, on) ? -1 : 0;
 }
 int vx_get_link_pipeline(void* s, int* blocks_per_sm) {
   CVoxelyze& vx = H(s)->vx;

@@ -49,6 +49,9 @@ struct VxImpl {
   bool state_dirty = true;   // host mirror edited
   bool device_ahead = false; // device state newer than the mirror
   bool nearby_dirty = true;  // collision lattice lists need regeneration
+  // materials or externals edited since the last step: Poisson caches the FP32C voxel pass filled
+  // ahead of time (VXG_VF_PSTRAIN_EAGER) may differ from what the lazy fill would give now
+  bool eager_stale = false;
   // per-step actuation handed to the engine (vxg_set_actuation); re-sent after topology changes
   int act_mode = 0;
   double act_amp = 0, act_freq = 0;

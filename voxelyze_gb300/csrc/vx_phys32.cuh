@@ -401,6 +401,9 @@ VX_HD void kahan_add(float& sum, float& comp, float x) {
   sum = t;
 }
 
+// FUSE_POIS: fill the Poisson-strain cache for the next step's link pass here, from this step's
+// link strains (which no later kernel of the step changes), instead of in a separate pre-pass
+template <bool FUSE_POIS>
 VX_HDN void voxel_update(const View& S, int v, float dt) {
   const vx64::View& B = S.B;
   const int nv = B.nv, nl = B.nl;
@@ -534,8 +537,20 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   st3(S.ang, nv, v, ang);
   S.Q[v] = make_float4(q.w, q.x, q.y, q.z);
   stq(S.qc, nv, v, qc);
-  B.vflags[v] = (flags & ~(uint32_t)VXG_VF_STATIC_FRICTION) | (staticF ? VXG_VF_STATIC_FRICTION : 0u) |
-                VXG_VF_PSTRAIN_INVALID;
+  uint32_t nf = (flags & ~(uint32_t)(VXG_VF_STATIC_FRICTION | VXG_VF_PSTRAIN_EAGER)) |
+                (staticF ? VXG_VF_STATIC_FRICTION : 0u) | VXG_VF_PSTRAIN_INVALID;
+  if (FUSE_POIS && m.nu != 0) {
+    bool any = false;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) any |= lk[i] >= 0;
+    if (any) {
+      float p[3];
+      vx64::poisson_strain_links(B, v, lk, p);
+      st3(B.pStrain, nv, v, F3(p[0], p[1], p[2]));
+      nf = (nf & ~(uint32_t)VXG_VF_PSTRAIN_INVALID) | VXG_VF_PSTRAIN_EAGER;
+    }
+  }
+  B.vflags[v] = nf;
 }
 
 }  // namespace vx32

@@ -240,11 +240,12 @@ VX_HD float link_axial_strain(const View& S, int l, bool positiveEnd) {
 }
 
 // CVX_Voxel::strain(true)  VX_Voxel.cpp:300-334
-VX_HDN void poisson_strain(const View& S, int v, float out[3]) {
+// (the voxel's six link slots `lk`, in direction order, already loaded by the caller)
+VX_HDN void poisson_strain_links(const View& S, int v, const int lk[6], float out[3]) {
   float s[3] = {0, 0, 0};
   int nb[3] = {0, 0, 0};
   for (int i = 0; i < 6; ++i) {
-    int li = S.vlinks[i * S.nv + v];
+    int li = lk[i];
     if (li >= 0) {
       s[i / 2] += link_axial_strain(S, li, i % 2 == 1);
       nb[i / 2]++;
@@ -271,6 +272,11 @@ VX_HDN void poisson_strain(const View& S, int v, float out[3]) {
       if (!tension[i]) s[i] = value;
   }
   out[0] = s[0]; out[1] = s[1]; out[2] = s[2];
+}
+VX_HDN void poisson_strain(const View& S, int v, float out[3]) {
+  int lk[6];
+  for (int i = 0; i < 6; ++i) lk[i] = S.vlinks[i * S.nv + v];
+  poisson_strain_links(S, v, lk, out);
 }
 
 // CVX_Voxel::baseSize(axis)  VX_Voxel.h:89

@@ -35,12 +35,15 @@ constexpr int kBlock = 256;
 
 // ---------------------------------------------------------------------------------------------
 // kernels
+// REDO: also refill caches the FP32C voxel pass filled ahead of time (VXG_VF_PSTRAIN_EAGER), after
+// a host edit of what they depend on (externals, materials, link state)
+template <bool REDO>
 __global__ void k_poisson(View S) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= S.nv) return;
   if (S.ctl->halt) return;
   uint32_t f = S.vflags[v];
-  if (!(f & VXG_VF_PSTRAIN_INVALID)) return;
+  if (!(f & (REDO ? (VXG_VF_PSTRAIN_INVALID | VXG_VF_PSTRAIN_EAGER) : VXG_VF_PSTRAIN_INVALID))) return;
   if (S.vm[S.vmat[v]].nu == 0) return;
   bool any = false;
 #pragma unroll
@@ -51,7 +54,7 @@ __global__ void k_poisson(View S) {
   S.pStrain[v] = p[0];
   S.pStrain[S.nv + v] = p[1];
   S.pStrain[2 * S.nv + v] = p[2];
-  S.vflags[v] = f & ~(uint32_t)VXG_VF_PSTRAIN_INVALID;
+  S.vflags[v] = f & ~(uint32_t)(VXG_VF_PSTRAIN_INVALID | VXG_VF_PSTRAIN_EAGER);
 }
 
 __device__ __forceinline__ void block_max_to(unsigned* dst, float f) {
@@ -405,7 +408,7 @@ __global__ void __launch_bounds__(kLpT) k_link32p(vx32::View S, int ntiles) {
   if (diverged) B.ctl->diverged = 1;
 }
 
-template <bool RECOMMEND>
+template <bool RECOMMEND, bool FUSE_POIS>
 __global__ void __launch_bounds__(512) k_voxel32(vx32::View S, float dt_fixed, int parity, float fallback) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (S.B.ctl->halt) return;
@@ -421,7 +424,7 @@ __global__ void __launch_bounds__(512) k_voxel32(vx32::View S, float dt_fixed, i
     if (RECOMMEND) S.B.ctl->maxf[parity ^ 1] = 0u;
   }
   if (v >= S.B.nv) return;
-  vx32::voxel_update(S, v, dt);
+  vx32::voxel_update<FUSE_POIS>(S, v, dt);
 }
 // FP64 interchange fields <-> FP32C working state, one field per launch (only the fields the host
 // writes are converted on upload, only the fields it reads on download)
@@ -638,6 +641,10 @@ struct vxg_engine {
   int lp_fit[2] = {0, 0};
   int n_sm = 0;
   bool tab_poisson = false;  // some voxel material has nu != 0
+  // FP32C with nu != 0: the voxel pass fills the Poisson cache for the next step; a host edit since
+  // the last step makes the next batch refill those caches first (k_poisson<true>)
+  bool poisson_redo = true;
+  bool poisson_fuse = true;  // vxg_set_poisson_fusion
   // per-step actuation (vxg_set_actuation)
   int act_mode = 0;
   double act_amp = 0, act_freq = 0;
@@ -949,6 +956,7 @@ int vxg_set_field(vxg_engine* e, int f, const void* host, long long count) {
   long long n = (long long)d.comps * (d.per_link ? e->nl : e->nv);
   if (count != n) return fail(e, VXG_E_SIZE, "vxg_set_field: element count mismatch");
   if (n == 0) return VXG_OK;
+  e->poisson_redo = true;
   if (e->precision == VXG_FP32C && is_state_field(f)) {
     e->dirty64 |= 1u << f;   // the FP64 copy is now the newer one
     e->stale64 &= ~(1u << f);
@@ -985,6 +993,7 @@ int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const 
   if ((rc = upload_table(e, &e->d_vm, &e->n_vm, vm, n_vm))) return rc;
   if ((rc = upload_table(e, &e->d_lm, &e->n_lm, lm, n_lm))) return rc;
   if ((rc = upload_table(e, &e->d_ext, &e->n_ext, ext, n_ext))) return rc;
+  e->poisson_redo = true;
   e->tab_poisson = false;
   for (int k = 0; k < n_vm; ++k)
     if (vm[k].nu != 0.0f) e->tab_poisson = true;
@@ -1018,6 +1027,7 @@ int vxg_set_powf_table(vxg_engine* e, int slot, float /*exponent*/, const float*
     e->d_powtab = np;
     e->n_powslots = ns;
   }
+  e->poisson_redo = true;
   VXG_CK(cudaMemcpyAsync(e->d_powtab + per * slot, table, per * sizeof(float), cudaMemcpyHostToDevice, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
   rebuild_view(e);
@@ -1057,8 +1067,19 @@ static int lp_resident(vxg_engine* e, bool pois) {
   return std::max(1, e->n_sm) * bps;
 }
 
-// enqueue one step (no synchronisation); in timing mode `ev` holds this step's 4 events
-static void enqueue_step(vxg_engine* e, float dt, int parity, cudaEvent_t* ev = nullptr) {
+static bool fused_poisson(const vxg_engine* e) {
+  return e->precision == VXG_FP32C && e->tab_poisson && e->poisson_fuse;
+}
+// before a batch: the Poisson caches the FP32C voxel pass filled ahead, after a host edit
+static void poisson_refill(vxg_engine* e) {
+  if (fused_poisson(e) && e->poisson_redo && e->g.any_poisson && e->nv)
+    k_poisson<true><<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S);
+  e->poisson_redo = false;
+}
+
+// enqueue one step (no synchronisation); in timing mode `ev` holds this step's 4 events.  `first`:
+// the first step of a batch or of a captured chunk.
+static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEvent_t* ev = nullptr) {
   const View& S = e->S;
   bool rec = dt < 0;
   const int bl = e->blk_link, bv = e->blk_voxel;
@@ -1072,7 +1093,10 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, cudaEvent_t* ev = 
       else k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(S);
     }
   }
-  if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S);
+  // FP32C fills the cache in the voxel pass; its pre-pass runs once per batch (for caches the host
+  // invalidated) and then finds nothing to do
+  if (e->g.any_poisson && e->nv && (first || !fused_poisson(e)))
+    k_poisson<false><<<grid_for(e->nv), kBlock, 0, e->stream>>>(S);
   if (e->precision == VXG_FP32C) {
     if (e->nl) {
       const bool pois = e->tab_poisson;
@@ -1091,8 +1115,13 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, cudaEvent_t* ev = 
     }
     if (ev) cudaEventRecord(ev[1], e->stream);
     if (ev) cudaEventRecord(ev[2], e->stream);
-    if (rec) k_voxel32<true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
-    else k_voxel32<false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+    if (fused_poisson(e)) {
+      if (rec) k_voxel32<true, true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+      else k_voxel32<false, true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+    } else {
+      if (rec) k_voxel32<true, false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+      else k_voxel32<false, false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+    }
     if (ev) cudaEventRecord(ev[3], e->stream);
     return;
   }
@@ -1112,7 +1141,7 @@ static int capture(vxg_engine* e, int n, float dt, cudaGraphExec_t* out) {
   if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
   cudaGraph_t g;
   VXG_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-  for (int s = 0; s < n; ++s) enqueue_step(e, dt, s & 1);
+  for (int s = 0; s < n; ++s) enqueue_step(e, dt, s & 1, s == 0);
   VXG_CK(cudaStreamEndCapture(e->stream, &g));
   cudaError_t c = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
@@ -1138,6 +1167,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
   unsigned z2[2] = {0u, 0u};
   VXG_CK(cudaMemcpyAsync(e->ctl->maxf, z2, sizeof(z2), cudaMemcpyHostToDevice, e->stream));
+  poisson_refill(e);
   bool use_graph = e->timing != 1 && nsteps > 1;
   if (e->timing == 2) {
     for (int k = 0; k < 2; ++k)
@@ -1160,7 +1190,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
       }
       int full = nsteps / chunk;
       for (int k = 0; k < full; ++k) VXG_CK(cudaGraphLaunch(e->cgraph, e->stream));
-      for (int s = full * chunk; s < nsteps; ++s) enqueue_step(e, dt, s & 1);
+      for (int s = full * chunk; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == full * chunk);
     } else {
       if (!e->graph_valid || !e->graph || e->graph_n != nsteps || e->graph_dt != dt) {
         int rc = capture(e, nsteps, dt, &e->graph);
@@ -1179,10 +1209,10 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
       VXG_CK(cudaEventCreate(&x));
       e->tev.push_back(x);
     }
-    for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, &e->tev[(size_t)4 * s]);
+    for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == 0, &e->tev[(size_t)4 * s]);
     e->tev_used = nsteps;
   } else {
-    for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1);
+    for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == 0);
   }
   if (e->timing == 2) VXG_CK(cudaEventRecord(e->bev[1], e->stream));
   int h[4];
@@ -1290,7 +1320,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
     int n = std::min(K, nsteps - c * K);
     for (int s = 0; s < n; ++s) {
       k_tape_save<<<gboth, kBlock, 0, e->stream>>>(e->S, T, s);
-      enqueue_step(e, dt, s & 1);
+      enqueue_step(e, dt, s & 1, s == 0);
     }
     for (int s = n - 1; s >= 0; --s) {
       if (nl) k_adj_link_forces<<<glk, kBlock, 0, e->stream>>>(e->S, T, A, s);
@@ -1322,7 +1352,8 @@ int vxg_recommended_dt(vxg_engine* e, float* dt) {
   unsigned z = 0u;
   VXG_CK(cudaMemcpyAsync(&e->ctl->maxf[0], &z, 4, cudaMemcpyHostToDevice, e->stream));
   ensure32(e);
-  if (e->g.any_poisson && e->nv) k_poisson<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S);
+  poisson_refill(e);
+  if (e->g.any_poisson && e->nv) k_poisson<false><<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S);
   if (e->precision == VXG_FP32C) {
     if (e->nl) k_link32<true, false, false><<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V, 0);
     e->stale64 |= 1u << VXG_F_REST_LENGTH;
@@ -1459,6 +1490,15 @@ int vxg_set_link_pipeline(vxg_engine* e, int blocks_per_sm) {
   e->graph_valid = false;
   return VXG_OK;
 }
+int vxg_set_poisson_fusion(vxg_engine* e, int on) {
+  if (!e) return VXG_E_ARG;
+  if (e->poisson_fuse != (on != 0)) {
+    e->poisson_fuse = on != 0;
+    e->poisson_redo = true;  // caches filled ahead of time are refilled at the lazy point
+    e->graph_valid = false;
+  }
+  return VXG_OK;
+}
 int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm) {
   if (!e || !blocks_per_sm) return VXG_E_ARG;
   *blocks_per_sm = e->lp_bps;
@@ -1514,6 +1554,7 @@ int vxg_restore(vxg_engine* e, int slot) {
     e->dirty64 = 0;
     e->stale64 = all_state_bits();
   }
+  e->poisson_redo = true;
   return VXG_OK;
 }
 

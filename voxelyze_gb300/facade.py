@@ -254,6 +254,7 @@ _EXT_SIGS = {
     "autotune": (_i, [_p, _i, _f, _ip]),
     "set_link_pipeline": (_i, [_p, _i]),
     "get_link_pipeline": (_i, [_p, _ip]),
+    "set_poisson_fusion": (_i, [_p, _i]),
     "adjoint_com_x": (_i, [_p, _i, _f, _i, _ip, _i, _dp, _dp, _dp, _dp]),
 }
 
@@ -305,6 +306,11 @@ class Engine:
         """FP32C link pass: >0 pipelined kernel with that many resident blocks per SM, -1 as many
         as fit, 0 the one-thread-per-link kernel (default)."""
         self._ck(self.f["set_link_pipeline"](self.sim.h, blocks_per_sm))
+
+    def set_poisson_fusion(self, on: bool):
+        """FP32C, nu != 0: fill the Poisson-strain cache in the voxel pass (default) or in a
+        pre-pass before every link pass; the trajectories are identical."""
+        self._ck(self.f["set_poisson_fusion"](self.sim.h, 1 if on else 0))
 
     def link_pipeline(self) -> int:
         out = np.zeros(1, np.int32)
