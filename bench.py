@@ -2,11 +2,14 @@
 """Time-step throughput of the GB300 engine on the 128x128x64 multi-material lattice.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision fp32c|fp64]
+                    [--workload lattice|cantilever|porous|population]
 
 Workload (seeded, synthetic; no public dataset exists for this path): 128x128x64 grid, Bernoulli
 0.85 fill (largest 6-connected component kept: ~0.89 M voxels, ~2.25 M links), 4 bilinear
 materials (E log-uniform 1e5..1e7 Pa, rho 1000..3000, nu 0.3), gravity and floor, 1 cm voxels,
-dt = recommendedTimeStep() at t = 0, then fixed.  A bench step is one doTimeStep.
+dt = recommendedTimeStep() at t = 0, then fixed.  A bench step is one doTimeStep.  --workload
+selects the other seeded scenes (40x8x8 cantilever; 64^3 porous body with collisions; 4,096
+independent bodies with in-step CTE actuation, whose CPU baseline steps the first 64 bodies).
 
 value  voxel-steps/s of the FP32-compensated path (--precision, default fp32c) with the scene
        resident on the GPU: K steps timed with CUDA events on the engine stream (first to last
@@ -159,17 +162,58 @@ def _peak_hbm():
 DIMS = (128, 128, 64)
 
 
-def build_lattice(sim_factory):
+class Workload:
+    """One seeded synthetic scene of the benchmark set; ``scene()`` builds the full case and
+    ``cpu_sample()`` the bounded sample the CPU baseline steps (the full scene unless stated)."""
+
+    def __init__(self, name, metric, desc, scene, cpu_sample=None, actuation=None, sample_desc=None):
+        self.name, self.metric, self.desc = name, metric, desc
+        self.scene = scene
+        self.cpu_sample = cpu_sample or scene
+        self.actuation = actuation            # (amplitude, frequency) of in-step CTE actuation
+        self.sample_desc = sample_desc
+
+
+def workloads():
     from voxelyze_gb300 import scenes as S
 
-    sc = S.lattice(*DIMS)
+    d = DIMS
+    return {
+        "lattice": Workload(
+            "lattice", "voxel-steps/s at 1M voxels (128x128x64 multi-material lattice)",
+            "lattice %dx%dx%d, fill 0.85, 4 bilinear materials, nu 0.3, gravity+floor, 1 cm" % d,
+            lambda: S.lattice(*DIMS)),
+        "cantilever": Workload(
+            "cantilever", "voxel-steps/s (40x8x8 cantilever)",
+            "cantilever 40x8x8, 5 mm, E 1 MPa, x=0 face fixed, -1 N per tip voxel", lambda: S.cantilever(40, 8, 8)),
+        "porous": Workload(
+            "porous", "voxel-steps/s (64^3 porous body, collisions)",
+            "porous 64^3 (sigma 3, void 0.4), nu 0.35, dropped 2 voxels onto the floor, gravity, collisions, "
+            "friction 1.0/0.5", lambda: S.porous(64)),
+        "population": Workload(
+            "population", "voxel-steps/s (4,096 independent bodies)",
+            "4,096 bodies, sides 4..24, occupancy 0.6, passive/active CTE materials, floor+gravity, friction "
+            "1.0/0.5, ambient temperature 0.1 sin(2 pi 2 t) applied inside every step",
+            lambda: S.population(4096), cpu_sample=lambda: S.population(64), actuation=(0.1, 2.0),
+            sample_desc="the first 64 bodies of the same generator"),
+    }
+
+
+def build_scene(sim_factory, sc):
+    from voxelyze_gb300 import scenes as S
+
     sim = sim_factory(sc.voxel_size)
     S.apply(sc, sim)
-    return sc, sim
+    return sim
 
 
-def cpu_oracle_rate(sc, threads: int, budget_s: float, steps_cap: int | None = None):
-    """Voxel-steps/s of the oracle (C-library math, `threads` OpenMP threads) on `sc`."""
+def cpu_oracle_rate(sc, threads: int, budget_s: float, steps_cap: int | None = None, actuation=None):
+    """Voxel-steps/s of the oracle (C-library math, `threads` OpenMP threads) on `sc`, over exactly
+    `steps_cap` steps if given, else over as many steps as fit in `budget_s` seconds; with
+    `actuation` = (amplitude, frequency), setAmbientTemperature(a sin(2 pi f t), true) before each
+    step, as the reference's user loop would call it."""
+    import math
+
     from voxelyze_gb300 import facade as F, scenes as S
 
     lib = C.CDLL(os.path.join(ROOT, "oracle", "_build", "libvxoracle.so"))
@@ -178,13 +222,19 @@ def cpu_oracle_rate(sc, threads: int, budget_s: float, steps_cap: int | None = N
     S.apply(sc, sim)
     lib.vxo_set_threads(C.c_void_p(sim.h), threads)
     dt = sim.recommended_time_step()
-    sim.do_time_step(dt)  # warm
+
+    def step(k):
+        if actuation:
+            sim.set_ambient_temperature(float(actuation[0] * math.sin(2 * math.pi * actuation[1] * k * dt)), True)
+        sim.do_time_step(dt)
+
+    step(0)  # warm
     n, t0 = 0, time.perf_counter()
     while True:
-        sim.do_time_step(dt)
+        step(n + 1)
         n += 1
         el = time.perf_counter() - t0
-        if el >= budget_s or (steps_cap and n >= steps_cap):
+        if (n >= steps_cap) if steps_cap else (el >= budget_s):
             break
     return sim.voxel_count() * n / el, n, el
 
@@ -192,20 +242,20 @@ def cpu_oracle_rate(sc, threads: int, budget_s: float, steps_cap: int | None = N
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    from voxelyze_gb300 import scenes as S
-
-    sc = S.lattice(*DIMS)
+    W = workloads()[args.workload]
+    sc = W.cpu_sample()
     cores = os.cpu_count() or 1
-    # warmup and timed steps, each one doTimeStep of the full lattice on all host cores
-    rate_w, _, _ = cpu_oracle_rate(sc, cores, 0.0, steps_cap=max(1, args.warmup))
-    rate, n, el = cpu_oracle_rate(sc, cores, 0.0, steps_cap=max(1, args.steps))
-    line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": n,
+    # warmup and timed steps, each one doTimeStep of the sample on all host cores
+    cpu_oracle_rate(sc, cores, 0.0, steps_cap=max(1, args.warmup), actuation=W.actuation)
+    rate, n, el = cpu_oracle_rate(sc, cores, 0.0, steps_cap=max(1, args.steps), actuation=W.actuation)
+    sample = f"{n} doTimeStep calls of the {'full ' if W.sample_desc is None else ''}{W.name}"
+    if W.sample_desc:
+        sample += f" ({W.sample_desc}, {sc.n_voxels} voxels)"
+    line = {"metric": W.metric, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": n,
             "warmup": args.warmup, "ms_per_step": 1e3 * el / n, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "lattice 128x128x64, fill 0.85, 4 bilinear materials, nu 0.3, gravity+floor",
-                       "voxels": sc.n_voxels, "precision": "fp64 CPU, C-library math"},
-            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{n} doTimeStep calls of the full 128x128x64 lattice"},
+            "config": {"workload": W.desc, "voxels": sc.n_voxels, "precision": "fp64 CPU, C-library math"},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -216,6 +266,9 @@ def _timed(lib, sim, steps, dt, local, barrier):
     split.  Returns both and the clocks sampled during the first."""
     h = C.c_void_p(sim.h)
     tm = (C.c_float * 4)()
+    cnt = (C.c_longlong * 8)()
+    lib.vx_counters(h, cnt, 8)
+    launches0 = cnt[6]
     lib.vx_enable_timing(h, 2)
     barrier()
     with _Clocks(local) as clk:
@@ -225,18 +278,21 @@ def _timed(lib, sim, steps, dt, local, barrier):
         raise RuntimeError(f"diverged after {done} steps")
     lib.vx_step_timing(h, tm)
     total_ms = float(tm[0])
+    lib.vx_counters(h, cnt, 8)
+    launches = int(cnt[6] - launches0)
     lib.vx_enable_timing(h, 1)
     if sim.do_time_steps(steps, dt) != steps:
         raise RuntimeError("diverged in the per-pass timing run")
     lib.vx_enable_timing(h, 0)
     lib.vx_step_timing(h, tm)
     _, link_ms, col_ms, vox_ms = [float(x) for x in tm]
-    return {"total_ms": total_ms, "link_ms": link_ms, "collide_ms": col_ms, "voxel_ms": vox_ms, "clocks": clk.summary()}
+    return {"total_ms": total_ms, "link_ms": link_ms, "collide_ms": col_ms, "voxel_ms": vox_ms, "clocks": clk.summary(),
+            "launches": launches}
 
 
 def run_ours(args, world, rank, local):
     import voxelyze_gb300 as vg
-    from voxelyze_gb300 import roofline as R
+    from voxelyze_gb300 import facade as F, roofline as R
 
     if world > 1:
         import torch
@@ -247,12 +303,16 @@ def run_ours(args, world, rank, local):
 
     from voxelyze_gb300.replicas import aggregate_rate, barrier
 
+    W = workloads()[args.workload]
     lib = vg.library()
     lib.vx_step_timing.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
-    sc, sim64 = build_lattice(vg.Sim)
-    _, sim32 = build_lattice(vg.Sim)
-    if lib.vx_set_precision(C.c_void_p(sim32.h), 1) != 0:
-        raise RuntimeError("FP32C precision not available")
+    sc = W.scene()
+    sim64 = build_scene(vg.Sim, sc)
+    sim32 = build_scene(vg.Sim, sc)
+    F.Engine(sim32).set_precision(1)
+    if W.actuation:
+        for sim in (sim64, sim32):
+            F.Engine(sim).set_actuation(F.ACT_UNIFORM, *W.actuation)
     nv, nl = sim64.voxel_count(), sim64.link_count()
     dt = sim64.recommended_time_step()
     sim32.recommended_time_step()
@@ -271,70 +331,91 @@ def run_ours(args, world, rank, local):
     p64 = sim64.voxel_state()["pos"]
     p32 = sim32.voxel_state()["pos"]
     disp = p64 - sc.xyz * sc.voxel_size
-    err = {"steps": args.warmup + args.steps,
+    err = {"steps": args.warmup + 2 * args.steps,
            "rel_pos": float(np.abs(p32 - p64).max() / np.abs(p64).max()),
            "rel_disp": float(np.abs(p32 - p64).max() / max(np.abs(disp).max(), 1e-30))}
+    extra = {}
+    if sc.body is not None:  # per-body centre-of-mass displacement (both precisions agree)
+        off = np.concatenate([[0], np.cumsum(np.bincount(sc.body))]).astype(np.int32)
+        com0 = np.stack([np.bincount(sc.body, weights=sc.xyz[:, k] * sc.voxel_size) for k in range(3)], 1)
+        com0 /= np.bincount(sc.body)[:, None]
+        c32, c64 = F.Engine(sim32).body_com(off), F.Engine(sim64).body_com(off)
+        d32 = c32 - com0
+        extra["body_com_displacement"] = {"bodies": int(len(off) - 1), "mean_dx": float(d32[:, 0].mean()),
+                                          "mean_dz": float(d32[:, 2].mean()),
+                                          "max_abs_fp32c_minus_fp64": float(np.abs(c32 - c64).max())}
 
     # ---- end to end through the public C facade ----------------------------------------------
     import torch
 
     h = C.c_void_p(head.h)
+    if W.actuation:
+        F.Engine(head).set_actuation(F.ACT_OFF)  # the host sends the temperatures instead
     temps = torch.zeros(nv, dtype=torch.float32, pin_memory=True)
     pos = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
-    lib.vx_set_temperatures.argtypes = [C.c_void_p, C.c_void_p]
-    lib.vx_read_positions.argtypes = [C.c_void_p, C.c_void_p]
+    # raw pinned addresses (the facade binding declares typed pointers for numpy callers)
+    set_temps = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)(("vx_set_temperatures", lib))
+    read_pos = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)(("vx_read_positions", lib))
     e2e_steps = max(3, min(args.steps, 50))
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        if lib.vx_set_temperatures(h, temps.data_ptr()) != 0:
+        if set_temps(h, temps.data_ptr()) != 0:
             raise RuntimeError("vx_set_temperatures failed")
         if lib.vx_do_time_step(h, C.c_float(dt)) != 1:
             raise RuntimeError("e2e step diverged")
-        if lib.vx_read_positions(h, pos.data_ptr()) != 0:
+        if read_pos(h, pos.data_ptr()) != 0:
             raise RuntimeError("vx_read_positions failed")
     e2e_value, _, _ = aggregate_rate(nv * e2e_steps, time.perf_counter() - t0)
     barrier()
 
     # ---- roofline of the dominant pass of the headline precision ------------------------------
     fp32 = head is sim32
-    b = (R.fp32c_bytes if fp32 else R.fp64_bytes)(nv, nl, poisson=True)
+    poisson = any(m.nu != 0 for m in sc.materials)
+    b = (R.fp32c_bytes if fp32 else R.fp64_bytes)(nv, nl, poisson=poisson)
     kernel = "link" if t_head["link_ms"] >= t_head["voxel_ms"] else "voxel"
     k_ms = t_head[f"{kernel}_ms"]
     achieved = b[kernel] / (k_ms / 1e3) / 1e9
     peak, peak_kind = _peak_hbm()
     kname = f"k_{kernel}{'32' if fp32 else ''}"
-    label = f"k_poisson + {kname}" if kernel == "link" else kname
+    label = f"k_poisson + {kname}" if (kernel == "link" and not fp32 and poisson) else kname
+    traffic = R.measured_traffic(f"{'fp32c' if fp32 else 'fp64'}_{kernel}", nv, nl) \
+        if args.workload == "lattice" else None
     roof = {"bound": "hbm", "kernel": f"{label} ({'FP32C' if fp32 else 'FP64'} {kernel} pass)", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": b[kernel], "ms_per_launch": k_ms,
-            "traffic": R.measured_traffic(f"{'fp32c' if fp32 else 'fp64'}_{kernel}", nv, nl),
+            "algorithmic_bytes_per_launch": b[kernel], "ms_per_launch": k_ms, "traffic": traffic,
             "step_bytes": b["step"], "step_frac": b["step"] / (t_head["total_ms"] / args.steps / 1e3) / 1e9 / peak}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        rate, n, el = cpu_oracle_rate(sc, cores, args.cpu_seconds)
+        cs = W.cpu_sample()
+        rate, n, el = cpu_oracle_rate(cs, cores, args.cpu_seconds, actuation=W.actuation)
+        what = "the full scene" if W.sample_desc is None else f"{W.sample_desc}, {cs.n_voxels} voxels"
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{n} doTimeStep calls of the full lattice in {el:.1f} s (OpenMP, C-library math)"}
+               "sample": f"{n} doTimeStep calls of {what} in {el:.1f} s (OpenMP, C-library math)"}
 
     o = t_other
-    line = {"metric": METRIC, "value": t_head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+    line = {"metric": W.metric, "value": t_head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_head["total_ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if fp32 else "f64", "data": "synthetic",
-            "config": {"workload": "lattice %dx%dx%d, fill 0.85, 4 bilinear materials, nu 0.3, gravity+floor, 1 cm" % DIMS,
-                       "voxels": nv, "links": nl, "precision": args.precision, "parallelism": f"replicas x{world}",
-                       "l2": "state > 129 MB L2 (FP64 ~1 GB, FP32C ~0.6 GB), no flush", "dt": dt,
-                       "per_pass_ms": {"link": t_head["link_ms"], "voxel": t_head["voxel_ms"]},
+            "config": {"workload": W.desc, "voxels": nv, "links": nl, "precision": args.precision,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "state > 129 MB L2, no flush" if nv >= 500000 else
+                             "state partly L2-resident (small scene), no flush",
+                       "dt": dt,
+                       "per_pass_ms": {"link": t_head["link_ms"], "collide": t_head["collide_ms"],
+                                       "voxel": t_head["voxel_ms"]},
                        "other_precision": {"precision": "fp64" if fp32 else "fp32c", "value": o["value"],
                                            "ms_per_step": o["total_ms"] / args.steps,
-                                           "per_pass_ms": {"link": o["link_ms"], "voxel": o["voxel_ms"]}},
+                                           "per_pass_ms": {"link": o["link_ms"], "collide": o["collide_ms"],
+                                                           "voxel": o["voxel_ms"]}},
                        "fp32c_over_fp64": (t_head["value"] / o["value"]) if fp32 else (o["value"] / t_head["value"]),
-                       "fp32c_error_vs_fp64": err},
+                       "fp32c_error_vs_fp64": err, **extra},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * nv, "d2h_bytes_per_step": 24 * nv,
                     "steps": e2e_steps},
-            "clocks": t_head["clocks"], "gpu_launches": 3 * args.steps}
+            "clocks": t_head["clocks"], "gpu_launches": t_head["launches"]}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -353,6 +434,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dims", default="128,128,64", help="lattice size (smaller cases for profiling)")
+    ap.add_argument("--workload", default="lattice", choices=["lattice", "cantilever", "porous", "population"],
+                    help="lattice (the headline), cantilever, porous (collisions), population (4,096 bodies)")
     args = ap.parse_args()
     global DIMS
     DIMS = tuple(int(x) for x in args.dims.split(","))

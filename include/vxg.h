@@ -141,6 +141,7 @@ enum { VXG_C_TRANSCENDENTAL = 0, /* correctly rounded sin/cos/acos evaluations *
        VXG_C_POWF_MISS = 3,      /* powf arguments outside the tabulated range */
        VXG_C_REBUILDS = 4,       /* collision pair-list rebuilds */
        VXG_C_PAIRS = 5,          /* current number of collision pairs */
+       VXG_C_LAUNCHES = 6,       /* kernels the time step launched (graph replays count their kernels) */
        VXG_C_COUNT = 8 };
 
 int vxg_create(vxg_engine** out, int device, int precision);

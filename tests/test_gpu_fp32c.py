@@ -180,3 +180,34 @@ def test_fused_poisson_cache_matches_prepass(product_lib, edit):
         assert a.do_time_steps(40, dt) == b.do_time_steps(40, dt) == 40
         for x, y in zip(_dynamic_state(a), _dynamic_state(b)):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("friction", [False, True])
+def test_collisions_fp32c_tracks_fp64(product_lib, friction):
+    """The porous collision scene (config 3's generator at 20^3) dropped onto the floor with
+    collisions on: FP32C against FP64.  Both start from the same lattice, so the first pair list
+    is the same set; the contact forces are FP32 in FP32C (offsets from lattice offsets plus
+    displacement differences).  Without friction FP32C tracks FP64 closely; with friction the
+    static-friction latch at first floor contact (src/VX_Voxel.cpp:285-291) is ill-conditioned, so
+    the bound is looser."""
+    sc = S.porous(20, sigma=1.5, z_offset=0)  # on the floor from the start
+    if not friction:
+        for m in sc.materials:
+            m.mu_static = m.mu_kinetic = 0.0
+    a, b = _pair(product_lib, sc)
+    dt = a.recommended_time_step()
+    assert b.recommended_time_step() == pytest.approx(dt, rel=1e-6)
+    assert a.do_time_steps(1, dt) == b.do_time_steps(1, dt) == 1
+    pa, pb = a.collisions(), b.collisions()
+    assert len(pa) > 0 and np.array_equal(pa, pb)
+    for _ in range(6):
+        assert a.do_time_steps(100, dt) == b.do_time_steps(100, dt) == 100
+    rel_pos, rel_disp = _errors(a, b, sc)
+    na, nb = len(a.collisions()), len(b.collisions())
+    print(f"porous 20^3 with collisions, friction={friction}, 601 steps: rel pos err {rel_pos:.3e}, "
+          f"rel disp err {rel_disp:.3e}, pairs FP64 {na} FP32C {nb}")
+    assert abs(na - nb) <= max(2, na // 100)
+    if friction:
+        assert rel_pos <= 1e-3
+    else:
+        assert rel_pos <= 1e-5

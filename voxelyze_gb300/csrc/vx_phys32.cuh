@@ -442,6 +442,16 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
     F.z -= cg * (m.massInv * lin.z);
   }
   F.z += -m.mass * 9.80665f * m.gravMult;
+  if (flags & VXG_VF_COLLISIONS) {  // contact forces in the partner order of the contact list
+    int b = B.colOff[v], en = B.colOff[v + 1];
+    for (int k = b; k < en; ++k) {
+      int it = B.colItem[k];
+      int c = it >> 1;
+      float fx = B.colForce[3 * c], fy = B.colForce[3 * c + 1], fz = B.colForce[3 * c + 2];
+      if (it & 1) { fx = -fx; fy = -fy; fz = -fz; }
+      F.x -= fx; F.y -= fy; F.z -= fz;
+    }
+  }
   f3 fric = F;
   bool floorOn = flags & VXG_VF_FLOOR;
   bool staticF = flags & VXG_VF_STATIC_FRICTION;

@@ -38,6 +38,14 @@ struct ColView {
   unsigned long long hcap_mask;
   const double* pos;
   const double* linMom;
+  // FP32C state (fp32 != 0): position = lattice index * voxel size + (d - c), momenta in FP32
+  int fp32;
+  const float4* P32;
+  const float* c32;
+  const float* lin32;
+  const int* vidx;
+  double s64;
+  float s32;
   const int* vmat;
   const uint32_t* vflags;
   const float* temp;
@@ -82,13 +90,21 @@ __device__ __forceinline__ unsigned long long hash64(unsigned long long k) {
 }
 __device__ __forceinline__ bool is_surface(const ColView& C, int v) { return !(C.vflags[v] & VXG_VF_INTERIOR); }
 
+// component k of voxel v's position in double: the FP64 state, or the FP32C state converted
+// exactly as a host read converts it (lattice origin + (d - c))
+__device__ __forceinline__ double cpos(const ColView& C, int v, int k) {
+  if (!C.fp32) return C.pos[k * C.nv + v];
+  float d = reinterpret_cast<const float*>(&C.P32[v])[k];
+  return C.vidx[k * C.nv + v] * C.s64 + ((double)d - (double)C.c32[k * C.nv + v]);
+}
+
 __global__ void c_check(ColView C) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (C.ctl->halt || C.ctl->diverged) return;
   if (v == 0 && C.cc->force_stale) C.cc->stale = 1;
   if (v >= C.nv || !is_surface(C, v)) return;
-  double dx = C.pos[v] - C.lastWatch[v], dy = C.pos[C.nv + v] - C.lastWatch[C.nv + v],
-         dz = C.pos[2 * C.nv + v] - C.lastWatch[2 * C.nv + v];
+  double dx = cpos(C, v, 0) - C.lastWatch[v], dy = cpos(C, v, 1) - C.lastWatch[C.nv + v],
+         dz = cpos(C, v, 2) - C.lastWatch[2 * C.nv + v];
   if (dx * dx + dy * dy + dz * dz > C.recalc2) C.cc->stale = 1;
 }
 
@@ -102,18 +118,18 @@ __global__ void c_clear(ColView C) {
 }
 
 __device__ __forceinline__ void cell_of(const ColView& C, int v, long long* c) {
-  c[0] = (long long)floor(C.pos[v] / C.cell);
-  c[1] = (long long)floor(C.pos[C.nv + v] / C.cell);
-  c[2] = (long long)floor(C.pos[2 * C.nv + v] / C.cell);
+  c[0] = (long long)floor(cpos(C, v, 0) / C.cell);
+  c[1] = (long long)floor(cpos(C, v, 1) / C.cell);
+  c[2] = (long long)floor(cpos(C, v, 2) / C.cell);
 }
 
 __global__ void c_insert(ColView C) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
   if (v >= C.nv || !is_surface(C, v)) return;
-  C.lastWatch[v] = (float)C.pos[v];
-  C.lastWatch[C.nv + v] = (float)C.pos[C.nv + v];
-  C.lastWatch[2 * C.nv + v] = (float)C.pos[2 * C.nv + v];
+  C.lastWatch[v] = (float)cpos(C, v, 0);
+  C.lastWatch[C.nv + v] = (float)cpos(C, v, 1);
+  C.lastWatch[2 * C.nv + v] = (float)cpos(C, v, 2);
   long long c[3];
   cell_of(C, v, c);
   unsigned long long k = cell_key(c[0], c[1], c[2]);
@@ -153,7 +169,7 @@ __device__ __forceinline__ bool in_sorted(const int* a, int n, int x) {
 // is (v, u) a collision pair of regenerateCollisions (Voxelyze.cpp:735-745)?
 __device__ __forceinline__ bool is_pair(const ColView& C, int v, int u) {
   int i = v < u ? v : u, j = v < u ? u : v;
-  double dx = C.pos[i] - C.pos[j], dy = C.pos[C.nv + i] - C.pos[C.nv + j], dz = C.pos[2 * C.nv + i] - C.pos[2 * C.nv + j];
+  double dx = cpos(C, i, 0) - cpos(C, j, 0), dy = cpos(C, i, 1) - cpos(C, j, 1), dz = cpos(C, i, 2) - cpos(C, j, 2);
   if (dx * dx + dy * dy + dz * dz > C.thr) return false;
   int b = C.nbOff[i], e = C.nbOff[i + 1];
   return !in_sorted(C.nbItem + b, e - b, j);
@@ -287,19 +303,74 @@ __device__ __forceinline__ double col_bsa(const ColView& C, int v) {
   return ((double)f * m.size[0] + (double)f * m.size[1] + (double)f * m.size[2]) / 3.0f;
 }
 
-// CVX_Collision::updateContactForce  VX_Collision.cpp:42-56
+// CVX_Collision::updateContactForce (VX_Collision.cpp:42-56) on the FP32C state, in FP32: the
+// offset between the two voxels is the exact lattice offset plus the difference of their
+// compensated displacements, so no two nearly equal absolute positions are subtracted
+__device__ __forceinline__ float3 c_off32(const ColView& C, int a, int b) {
+  const int nv = C.nv;
+  float4 da = C.P32[a], db = C.P32[b];
+  float r[3];
+  const float dd[3] = {db.x - da.x, db.y - da.y, db.z - da.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float lat = (float)(C.vidx[k * nv + b] - C.vidx[k * nv + a]) * C.s32;
+    float dc = C.c32[k * nv + b] - C.c32[k * nv + a];
+    r[k] = lat + (dd[k] - dc);
+  }
+  return make_float3(r[0], r[1], r[2]);
+}
+__device__ __forceinline__ float col_bsa32(const ColView& C, int v) {
+  const vxg_voxel_material& m = C.vm[C.vmat[v]];
+  return m.sizeAvgF * (1 + C.temp[v] * m.alphaCTE);
+}
+__device__ void c_contact32(const ColView& C, int c, int a, int b) {
+  const int nv = C.nv;
+  float3 o = c_off32(C, a, b);
+  float nom = (col_bsa32(C, a) + col_bsa32(C, b)) * 0.625f;
+  float len = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
+  float rel = nom - len;
+  float fx = 0, fy = 0, fz = 0;
+  if (rel > 0) {
+    float ux = o.x, uy = o.y, uz = o.z;
+    if (len > 0) {
+      float inv = 1.0f / len;
+      ux = inv * o.x; uy = inv * o.y; uz = inv * o.z;
+    }
+    const vxg_voxel_material& m1 = C.vm[C.vmat[a]];
+    const vxg_voxel_material& m2 = C.vm[C.vmat[b]];
+    float v1x = m1.massInv * C.lin32[a], v1y = m1.massInv * C.lin32[nv + a], v1z = m1.massInv * C.lin32[2 * nv + a];
+    float v2x = m2.massInv * C.lin32[b], v2y = m2.massInv * C.lin32[nv + b], v2z = m2.massInv * C.lin32[2 * nv + b];
+    float relVel = (v1x * ux + v1y * uy + v1z * uz) - (v2x * ux + v2y * uy + v2z * uz);
+    float k = C.pairStiff[c] * rel + C.pairDamp[c] * relVel;
+    fx = ux * k; fy = uy * k; fz = uz * k;
+  }
+  C.pairForce[3 * c] = fx;
+  C.pairForce[3 * c + 1] = fy;
+  C.pairForce[3 * c + 2] = fz;
+}
+
+// CVX_Collision::updateContactForce  VX_Collision.cpp:42-56, one pair per thread of a resident grid
+// (the pair count is known only on the device)
+__device__ __forceinline__ void c_contact64(const ColView& C, int c, int a, int b);
 __global__ void c_contact(ColView C) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (C.ctl->halt || C.ctl->diverged) return;
-  if (c == 0) {
+  const int npairs = C.cc->npairs, status = C.cc->status;  // thread 0 clears neither
+  if (t == 0) {
     if (C.cc->stale) C.cc->rebuilds += 1;
     C.cc->stale = 0;
     C.cc->force_stale = 0;
-    if (C.cc->status) atomicOr(&C.ctl->status, C.cc->status << 8);
+    if (status) atomicOr(&C.ctl->status, status << 8);
   }
-  if (c >= C.cc->npairs || C.cc->status) return;
-  int a = C.pairI[c], b = C.pairJ[c];
-  int nv = C.nv;
+  if (status) return;
+  for (int c = t; c < npairs; c += gridDim.x * blockDim.x) {
+    int a = C.pairI[c], b = C.pairJ[c];
+    if (C.fp32) c_contact32(C, c, a, b);
+    else c_contact64(C, c, a, b);
+  }
+}
+__device__ __forceinline__ void c_contact64(const ColView& C, int c, int a, int b) {
+  const int nv = C.nv;
   float ox = (float)(C.pos[b] - C.pos[a]), oy = (float)(C.pos[nv + b] - C.pos[nv + a]),
         oz = (float)(C.pos[2 * nv + b] - C.pos[2 * nv + a]);
   float nom = (float)((col_bsa(C, a) + col_bsa(C, b)) * 0.625f);
@@ -399,7 +470,10 @@ struct Collide {
     C.pcap = pcap;
     C.wcap = wcap;
     C.cc = cc;
-    grid_pairs = std::max(1, (pcap + 255) / 256);
+    int dev = 0, n_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    grid_pairs = std::max(1, std::min((pcap + 255) / 256, 4 * n_sm));
     return VXG_OK;
   }
   int set_nearby(int n, const int* off, const int* items, long long n_items, cudaStream_t s) {
@@ -423,7 +497,16 @@ struct Collide {
     C.nbItem = d_nb + n + 1;
     return VXG_OK;
   }
+  // FP32C engines: the collision stage reads the FP32C state (bind32 after bind)
+  void bind32(const vx32::View& V) {
+    C.fp32 = 1;
+    C.P32 = V.P;
+    C.c32 = V.c;
+    C.lin32 = V.lin;
+    C.vidx = V.B.vidx;
+  }
   void bind(View& S) {
+    C.fp32 = 0;
     C.pos = S.pos;
     C.linMom = S.linMom;
     C.vmat = S.vmat;
@@ -435,23 +518,36 @@ struct Collide {
     S.colItem = C.watchItem;
     S.colForce = C.pairForce;
   }
-  void enqueue(const vxg_globals& g, cudaStream_t s) {
-    if (!buf || !C.nbOff) return;
+  void set_globals(const vxg_globals& g) {
     float watchVx = 2 * g.boundingRadius + g.watchDistance;
     float watchMm = (float)(g.voxSize * watchVx);
     float recalc = (float)(g.voxSize * g.watchDistance / 2);
     C.thr = (double)(watchMm * watchMm);
     C.recalc2 = (double)(recalc * recalc);
     C.cell = (double)watchMm * 1.001;
+    C.s64 = g.voxSize;
+    C.s32 = (float)g.voxSize;
+  }
+  void enqueue_rebuild(cudaStream_t s) {
     int gv = std::max(1, (nv + 255) / 256);
-    c_check<<<gv, 256, 0, s>>>(C);
     c_clear<<<256, 256, 0, s>>>(C);
     c_insert<<<gv, 256, 0, s>>>(C);
     c_count<<<gv, 256, 0, s>>>(C);
     c_scan<<<1, 1024, 0, s>>>(C);
     c_fill<<<std::max(1, (nv + 127) / 128), 128, 0, s>>>(C);  // 128 threads: 512 B of partners each
     c_watch<<<gv, 256, 0, s>>>(C);
+  }
+  // Launches the stage on stream s; returns the number of kernels launched.  The rebuild kernels
+  // exit at once unless c_check found the pair list stale.  (A conditional graph node around them
+  // measured slower than these early exits on GB300.)
+  int enqueue(const vxg_globals& g, cudaStream_t s) {
+    if (!buf || !C.nbOff) return 0;
+    set_globals(g);
+    int gv = std::max(1, (nv + 255) / 256);
+    c_check<<<gv, 256, 0, s>>>(C);
+    enqueue_rebuild(s);
     c_contact<<<grid_pairs, 256, 0, s>>>(C);
+    return 8;
   }
   int get_pairs(int* out, int cap, int* n, cudaStream_t s) {
     *n = 0;

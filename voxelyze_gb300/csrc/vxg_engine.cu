@@ -645,6 +645,8 @@ struct vxg_engine {
   // the last step makes the next batch refill those caches first (k_poisson<true>)
   bool poisson_redo = true;
   bool poisson_fuse = true;  // vxg_set_poisson_fusion
+  // kernels launched by the time step (a graph replay counts the kernels it holds)
+  long long n_launch = 0, graph_kernels = 0, cgraph_kernels = 0;
   // per-step actuation (vxg_set_actuation)
   int act_mode = 0;
   double act_amp = 0, act_freq = 0;
@@ -731,6 +733,7 @@ static void rebuild_view(vxg_engine* e) {
   e->col.bind(S);
   e->V.B = S;
   e->V.s = (float)e->g.voxSize;
+  if (e->precision == VXG_FP32C) e->col.bind32(e->V);
   e->graph_valid = false;
 }
 
@@ -1036,7 +1039,6 @@ int vxg_set_powf_table(vxg_engine* e, int slot, float /*exponent*/, const float*
 
 int vxg_set_globals(vxg_engine* e, const vxg_globals* g) {
   if (!e || !g) return VXG_E_ARG;
-  if (e->precision == VXG_FP32C && g->collisions) return fail(e, VXG_E_ARG, "collisions run in FP64 precision only");
   e->g = *g;
   e->have_globals = true;
   e->V.s = (float)g->voxSize;
@@ -1072,8 +1074,10 @@ static bool fused_poisson(const vxg_engine* e) {
 }
 // before a batch: the Poisson caches the FP32C voxel pass filled ahead, after a host edit
 static void poisson_refill(vxg_engine* e) {
-  if (fused_poisson(e) && e->poisson_redo && e->g.any_poisson && e->nv)
+  if (fused_poisson(e) && e->poisson_redo && e->g.any_poisson && e->nv) {
     k_poisson<true><<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S);
+    e->n_launch += 1;
+  }
   e->poisson_redo = false;
 }
 
@@ -1085,6 +1089,9 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   const int bl = e->blk_link, bv = e->blk_voxel;
   const int gl = grid_of(e->nl, bl), gv = grid_of(e->nv, bv);
   if (ev) cudaEventRecord(ev[0], e->stream);
+  // kernels this step launches (or, under capture, records)
+  long long nk = 1 + (e->nl ? 1 : 0) + (e->act_mode && e->nv ? 1 + (e->nl ? 1 : 0) : 0) +
+                 (e->g.any_poisson && e->nv && (first || !fused_poisson(e)) ? 1 : 0);
   if (e->act_mode && e->nv) {
     k_actuate<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S, e->act_amp, e->act_freq, e->act_mode == 2 ? e->d_phase : nullptr,
                                                         e->precision == VXG_FP32C ? 1 : 0);
@@ -1114,7 +1121,9 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
       }
     }
     if (ev) cudaEventRecord(ev[1], e->stream);
+    if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream);
     if (ev) cudaEventRecord(ev[2], e->stream);
+    e->n_launch += nk;
     if (fused_poisson(e)) {
       if (rec) k_voxel32<true, true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
       else k_voxel32<false, true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
@@ -1130,8 +1139,9 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
     else k_link<false, true><<<gl, bl, 0, e->stream>>>(S, parity);
   }
   if (ev) cudaEventRecord(ev[1], e->stream);
-  if (e->g.collisions) e->col.enqueue(e->g, e->stream);
+  if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream);
   if (ev) cudaEventRecord(ev[2], e->stream);
+  e->n_launch += nk;
   if (rec) k_voxel<true><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
   else k_voxel<false><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
   if (ev) cudaEventRecord(ev[3], e->stream);
@@ -1141,7 +1151,12 @@ static int capture(vxg_engine* e, int n, float dt, cudaGraphExec_t* out) {
   if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
   cudaGraph_t g;
   VXG_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  const long long before = e->n_launch;
   for (int s = 0; s < n; ++s) enqueue_step(e, dt, s & 1, s == 0);
+  const long long in_graph = e->n_launch - before;
+  e->n_launch = before;  // counted per replay
+  if (out == &e->cgraph) e->cgraph_kernels = in_graph;
+  else e->graph_kernels = in_graph;
   VXG_CK(cudaStreamEndCapture(e->stream, &g));
   cudaError_t c = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
@@ -1190,6 +1205,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
       }
       int full = nsteps / chunk;
       for (int k = 0; k < full; ++k) VXG_CK(cudaGraphLaunch(e->cgraph, e->stream));
+      e->n_launch += full * e->cgraph_kernels;
       for (int s = full * chunk; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == full * chunk);
     } else {
       if (!e->graph_valid || !e->graph || e->graph_n != nsteps || e->graph_dt != dt) {
@@ -1201,6 +1217,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
         e->graph_valid = true;
       }
       VXG_CK(cudaGraphLaunch(e->graph, e->stream));
+      e->n_launch += e->graph_kernels;
     }
   } else if (e->timing == 1) {
     size_t need = (size_t)4 * nsteps;
@@ -1653,6 +1670,7 @@ int vxg_counters(vxg_engine* e, long long* out, int n) {
   VXG_CK(cudaStreamSynchronize(e->stream));
   h[VXG_C_REBUILDS] = (unsigned long long)e->col.rebuilds();
   h[VXG_C_PAIRS] = (unsigned long long)e->col.pairs(e->stream);
+  h[VXG_C_LAUNCHES] = (unsigned long long)e->n_launch;
   for (int i = 0; i < n && i < VXG_C_COUNT; ++i) out[i] = (long long)h[i];
   return VXG_OK;
 }

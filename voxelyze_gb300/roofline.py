@@ -46,18 +46,23 @@ def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
 #                         + 80 written, flags 4+4, material id 4, external id 4, 6 link ids 24,
 #                         lattice z 4, temperature 4                                     = 208 B
 #             per link  : the force and moment each end gathers, 2 x 24                   =  48 B
+#   Poisson cache (nu != 0), filled by the voxel pass for the next step: cached strain 12 B written
+#                         per voxel, strain and strain ratio 8 B per link gathered
 FP32C_LINK_PER_LINK = 188
 FP32C_LINK_PER_VOXEL = 32
 FP32C_LINK_PER_VOXEL_POISSON = 12
 FP32C_VOXEL_PER_VOXEL = 208
 FP32C_VOXEL_PER_LINK = 48
+FP32C_VOXEL_PER_VOXEL_POISSON = 12
+FP32C_VOXEL_PER_LINK_POISSON = 8
 
 
 def fp32c_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
     link = FP32C_LINK_PER_LINK * n_links + FP32C_LINK_PER_VOXEL * n_voxels
-    if poisson:
-        link += (FP64_POISSON_PER_VOXEL + FP32C_LINK_PER_VOXEL_POISSON) * n_voxels + FP64_POISSON_PER_LINK * n_links
     voxel = FP32C_VOXEL_PER_VOXEL * n_voxels + FP32C_VOXEL_PER_LINK * n_links
+    if poisson:
+        link += FP32C_LINK_PER_VOXEL_POISSON * n_voxels
+        voxel += FP32C_VOXEL_PER_VOXEL_POISSON * n_voxels + FP32C_VOXEL_PER_LINK_POISSON * n_links
     return {"link": link, "voxel": voxel, "step": link + voxel}
 
 
