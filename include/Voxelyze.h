@@ -1,11 +1,13 @@
 // CVoxelyze: the drop-in simulation object (same public interface as the reference's
 // include/Voxelyze.h:45-134).  Scene building runs on the host in the reference's voxel and link
 // order; doTimeStep runs on the GPU through the vxg engine (include/vxg.h).  Not thread-safe, like
-// the reference.  JSON scene I/O and the PARDISO linear solve of the reference are not provided.
+// the reference.  *.vxl.json scene files are read and written in the reference's format (without
+// its rapidjson dependency); the PARDISO linear solve of the reference is not provided.
 #ifndef VX_GB300_VOXELYZE_H
 #define VX_GB300_VOXELYZE_H
 
 #include <list>
+#include <string>
 #include <vector>
 
 #include "VX_Collision.h"
@@ -29,11 +31,16 @@ class CVoxelyze {
   enum precisionMode { PRECISION_FP64 = 0, PRECISION_FP32C = 1 };
 
   CVoxelyze(double voxelSize = DEFAULT_VOXEL_SIZE);
+  CVoxelyze(const char* jsonFilePath);  // Voxelyze.h:70
   ~CVoxelyze();
   CVoxelyze(CVoxelyze& VIn);
   CVoxelyze& operator=(CVoxelyze& VIn);
 
   void clear();
+  // *.vxl.json scene files (Voxelyze.cpp:61-241): the scene's voxel size, materials, voxels and
+  // externals; the state is not saved
+  bool loadJSON(const char* jsonFilePath);
+  bool saveJSON(const char* jsonFilePath);
 
   bool doTimeStep(float dt = -1.0f);
   float recommendedTimeStep() const;
@@ -119,6 +126,8 @@ class CVoxelyze {
   void replaceVoxel(CVX_MaterialVoxel* m, int x, int y, int z);
   CVX_Link* addLink(int x, int y, int z, CVX_Voxel::linkDirection d);
   void removeLink(int x, int y, int z, CVX_Voxel::linkDirection d);
+  bool readJSON(const void* documentRoot);  // a parsed vxjson::Value (vx_json.h)
+  std::string writeJSON();
 
   // host mirror synchronisation
   void syncDown() const;       // device -> host mirror if the device is ahead

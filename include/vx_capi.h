@@ -40,6 +40,8 @@ int vx_do_time_step(void* s, float dt);                     /* doTimeStep: 1 ok,
 int vx_do_time_steps(void* s, int n, float dt);             /* n doTimeStep calls in one GPU batch; steps completed */
 float vx_recommended_time_step(void* s);                    /* src/Voxelyze.cpp:286-311 */
 void vx_reset_time(void* s);                                /* src/Voxelyze.cpp:313-321 */
+int vx_load_json(void* s, const char* path);                /* CVoxelyze::loadJSON  src/Voxelyze.cpp:61-77, 95-162 */
+int vx_save_json(void* s, const char* path);                /* CVoxelyze::saveJSON  src/Voxelyze.cpp:79-93, 164-241 */
 float vx_current_time(void* s);                             /* CVoxelyze::currentTime   include/Voxelyze.h:138 */
 /* full state dumps, layouts as in oracle/facade.h: voxels d13/f5/i2, links d22/f6/i6 */
 int vx_get_voxel_state(void* s, double* d13, float* f5, int* i2);

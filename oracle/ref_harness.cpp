@@ -167,6 +167,8 @@ int vxr_voxel_set_temperature(void* s, int v, float t) {
 }
 
 int vxr_do_time_step(void* s, float dt) { return S(s)->vx.doTimeStep(dt) ? 1 : 0; }
+int vxr_load_json(void* s, const char* path) { return S(s)->vx.loadJSON(path) ? 1 : 0; }
+int vxr_save_json(void* s, const char* path) { return S(s)->vx.saveJSON(path) ? 1 : 0; }
 int vxr_do_time_steps(void* s, int n, float dt) {
   for (int i = 0; i < n; ++i)
     if (!S(s)->vx.doTimeStep(dt)) return i;

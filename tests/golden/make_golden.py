@@ -1,6 +1,7 @@
 """Generates the golden fixtures in this directory from the REFERENCE library compiled from its own
 sources (oracle/build_ref.sh -> oracle/_ref/libvxref.so).  Run here, where the reference tree
-exists:  python tests/golden/make_golden.py
+exists:  python tests/golden/make_golden.py        (all fixtures)
+         python tests/golden/make_golden.py json   (the scene file only)
 
 Each fixture holds the reference's full state after a known number of steps of one scene, either
 in full (small scenes) or as SHA-256 digests of the state bytes plus a sample of voxels (larger
@@ -53,8 +54,19 @@ SCENES = {
 }
 
 
+def save_scene_json(lib):
+    """scene_ref.vxl.json: CVoxelyze::saveJSON of the scene test_scene_json.build_scene makes."""
+    from test_scene_json import build_scene
+
+    sim = build_scene(lib, "vxr")
+    assert sim.save_json(os.path.join(HERE, "scene_ref.vxl.json"))
+
+
 def main():
     lib = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libvxref.so"))
+    save_scene_json(lib)
+    if sys.argv[1:] == ["json"]:
+        return
     meta = {"platform": platform.machine(), "libc": platform.libc_ver()[1], "scenes": {}}
     for name, (mk, steps, cps, mode, full) in SCENES.items():
         sc = mk()

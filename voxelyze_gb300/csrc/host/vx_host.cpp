@@ -1245,6 +1245,8 @@ int vx_do_time_step(void* s, float dt) {
 int vx_do_time_steps(void* s, int n, float dt) { return H(s)->vx.doTimeSteps(n, dt); }
 float vx_recommended_time_step(void* s) { return H(s)->vx.recommendedTimeStep(); }
 void vx_reset_time(void* s) { H(s)->vx.resetTime(); }
+int vx_load_json(void* s, const char* path) { return H(s)->vx.loadJSON(path) ? 1 : 0; }
+int vx_save_json(void* s, const char* path) { return H(s)->vx.saveJSON(path) ? 1 : 0; }
 float vx_current_time(void* s) { return H(s)->vx.currentTime(); }
 
 int vx_get_voxel_state(void* s, double* d, float* f, int* i) {

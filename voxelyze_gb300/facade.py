@@ -73,6 +73,13 @@ _SIGS = {
 }
 
 
+# scene-file entry points: in the product and the reference build, not in the oracle
+_OPT_SIGS = {
+    "load_json": (_i, [_p, C.c_char_p]),
+    "save_json": (_i, [_p, C.c_char_p]),
+}
+
+
 def bind(lib: C.CDLL, prefix: str) -> dict:
     """Resolve every facade symbol ``<prefix>_<name>`` in ``lib`` and set its ctypes signature."""
     fns = {}
@@ -81,6 +88,12 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
         fn.restype = res
         fn.argtypes = args
         fns[name] = fn
+    for name, (res, args) in _OPT_SIGS.items():
+        fn = getattr(lib, f"{prefix}_{name}", None)
+        if fn is not None:
+            fn.restype = res
+            fn.argtypes = args
+            fns[name] = fn
     return fns
 
 
@@ -198,6 +211,13 @@ class Sim:
 
     def reset_time(self):
         self.f["reset_time"](self.h)
+
+    # -- scene files (CVoxelyze::loadJSON / saveJSON) ---------------------------------------
+    def load_json(self, path: str) -> bool:
+        return self.f["load_json"](self.h, path.encode()) == 1
+
+    def save_json(self, path: str) -> bool:
+        return self.f["save_json"](self.h, path.encode()) == 1
 
     def current_time(self) -> float:
         return self.f["current_time"](self.h)
