@@ -133,6 +133,8 @@ class CVoxelyze {
   void syncDown() const;       // device -> host mirror if the device is ahead
   void markState() const;      // host mirror edited: upload before the next step
   void markTables();           // materials or externals changed
+  void markExternals();        // an existing external changed
+  bool pushPending() const;    // queued per-voxel temperatures -> device
   void markTopology();         // voxel or link added/removed
   bool flush();                // upload whatever is stale
 

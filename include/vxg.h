@@ -153,6 +153,13 @@ int vxg_set_field(vxg_engine* e, int field, const void* host, long long count);
 int vxg_get_field(vxg_engine* e, int field, void* host, long long count);
 int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const vxg_link_material* lm,
                    int n_lm, const vxg_external* ext, int n_ext);
+/* Uploads only the externals table (the layout and slot numbering of vxg_set_tables), after
+ * setForce / setMoment / setDisplacement on voxels that already have externals
+ * (include/VX_External.h:39-90); captured graphs stay valid while the table keeps its size. */
+int vxg_set_externals(vxg_engine* e, const vxg_external* ext, int n_ext);
+/* CVX_Voxel::setTemperature (src/VX_Voxel.cpp:108-114) for n voxels at once, on the device: their
+ * temperatures, then the rest lengths of their links.  Indices must be distinct. */
+int vxg_set_temperatures_sparse(vxg_engine* e, int n, const int* voxels, const float* temps);
 /* Tabulated powf(x, exponent) for every float x in [0.5, 2): 2^24 entries indexed by
  * (bits(x) - bits(0.5f)), computed on the host by the C library the reference links. */
 int vxg_set_powf_table(vxg_engine* e, int slot, float exponent, const float* table);

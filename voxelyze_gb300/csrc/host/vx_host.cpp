@@ -108,6 +108,21 @@ void CVoxelyze::markTables() {
   pimpl->tables_dirty = true;
   pimpl->eager_stale = true;
 }
+void CVoxelyze::markExternals() {
+  pimpl->ext_dirty = true;
+  pimpl->eager_stale = true;
+}
+bool CVoxelyze::pushPending() const {
+  VxImpl& I = *pimpl;
+  if (I.pend_voxel.empty()) return true;
+  int rc = I.eng ? vxg_set_temperatures_sparse(I.eng, (int)I.pend_voxel.size(), I.pend_voxel.data(), I.pend_temp.data())
+                 : VXG_E_STATE;
+  for (int v : I.pend_voxel) I.pend_slot[v] = -1;
+  I.pend_voxel.clear();
+  I.pend_temp.clear();
+  if (rc) { I.err = I.eng ? vxg_last_error(I.eng) : "no engine"; return false; }
+  return true;
+}
 void CVoxelyze::markTopology() {
   pimpl->topo_dirty = true;
   pimpl->tables_dirty = true;
@@ -469,9 +484,26 @@ static bool transfer(VxImpl& I, const FieldMap& f, bool up) {
 void CVoxelyze::syncDown() const {
   VxImpl& I = *pimpl;
   if (!I.device_ahead || !I.eng) return;
+  pushPending();
   for (const FieldMap& f : kState) transfer(I, f, false);
   vxg_get_field(I.eng, VXG_F_TIME, &I.time, 1);
   I.device_ahead = false;
+}
+
+// one voxel's externals as the engine table holds them (include/VX_External.h:92-97)
+static vxg_external external_entry(const CVX_External& e) {
+  vxg_external d;
+  std::memset(&d, 0, sizeof(d));
+  for (int k = 0; k < 6; ++k)
+    if (e.isFixed((dofComponent)(1 << k))) d.dof |= 1 << k;
+  Vec3D<float> f = e.force(), m = e.moment();
+  Vec3D<double> t = e.translation();
+  d.force[0] = f.x; d.force[1] = f.y; d.force[2] = f.z;
+  d.moment[0] = m.x; d.moment[1] = m.y; d.moment[2] = m.z;
+  d.translation[0] = t.x; d.translation[1] = t.y; d.translation[2] = t.z;
+  Quat3D<double> q = e.rotationQuat();
+  d.rotq[0] = q.w; d.rotq[1] = q.x; d.rotq[2] = q.y; d.rotq[3] = q.z;
+  return d;
 }
 
 bool CVoxelyze::flush() {
@@ -576,19 +608,13 @@ bool CVoxelyze::flush() {
     }
     std::vector<vxg_external> ex;
     std::vector<int> vext((size_t)nv, -1);
+    I.ext_voxels.clear();
     for (int i = 0; i < nv; ++i) {
       CVX_External* e = voxelsList[i]->ext;
       if (!e) continue;
-      vxg_external d;
-      std::memset(&d, 0, sizeof(d));
-      d.dof = e->dofFixed;
-      d.force[0] = e->extForce.x; d.force[1] = e->extForce.y; d.force[2] = e->extForce.z;
-      d.moment[0] = e->extMoment.x; d.moment[1] = e->extMoment.y; d.moment[2] = e->extMoment.z;
-      d.translation[0] = e->extTranslation.x; d.translation[1] = e->extTranslation.y; d.translation[2] = e->extTranslation.z;
-      Quat3D<double> q = e->rotationQuat();
-      d.rotq[0] = q.w; d.rotq[1] = q.x; d.rotq[2] = q.y; d.rotq[3] = q.z;
       vext[i] = (int)ex.size();
-      ex.push_back(d);
+      ex.push_back(external_entry(*e));
+      I.ext_voxels.push_back(i);
     }
     if (vxg_set_tables(I.eng, vm.data(), (int)vm.size(), lm.data(), (int)lm.size(), ex.data(), (int)ex.size())) {
       I.err = vxg_last_error(I.eng);
@@ -605,7 +631,16 @@ bool CVoxelyze::flush() {
     g.fallback_freq2 = fallback;
     vxg_set_globals(I.eng, &g);
     I.tables_dirty = false;
+    I.ext_dirty = false;
   }
+  if (I.ext_dirty) {  // externals edited, none added: their table only
+    std::vector<vxg_external> ex;
+    ex.reserve(I.ext_voxels.size());
+    for (int i : I.ext_voxels) ex.push_back(external_entry(*voxelsList[i]->ext));
+    if (vxg_set_externals(I.eng, ex.data(), (int)ex.size())) { I.err = vxg_last_error(I.eng); return false; }
+    I.ext_dirty = false;
+  }
+  if (!pushPending()) return false;
   if (I.state_dirty) {
     for (const FieldMap& f : kState)
       if (!transfer(I, f, true)) return false;
@@ -902,6 +937,20 @@ float CVX_Voxel::temperature() {
   return VXI.vf[VF_TEMP][idx];
 }
 void CVX_Voxel::setTemperature(float t) {  // VX_Voxel.cpp:108-114
+  VxImpl& I = *vx->pimpl;
+  if (I.device_ahead && I.eng && !I.state_dirty && !I.topo_dirty) {
+    // the device holds the newer state: queue the change instead of a full round trip
+    if (I.pend_slot.size() < vx->voxelsList.size()) I.pend_slot.resize(vx->voxelsList.size(), -1);
+    int& slot = I.pend_slot[idx];
+    if (slot < 0) {
+      slot = (int)I.pend_voxel.size();
+      I.pend_voxel.push_back(idx);
+      I.pend_temp.push_back(t);
+    } else {
+      I.pend_temp[slot] = t;
+    }
+    return;
+  }
   vx->syncDown();
   VXI.vf[VF_TEMP][idx] = t;
   for (int i = 0; i < 6; i++)

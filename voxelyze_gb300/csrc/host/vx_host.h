@@ -52,6 +52,14 @@ struct VxImpl {
   // materials or externals edited since the last step: Poisson caches the FP32C voxel pass filled
   // ahead of time (VXG_VF_PSTRAIN_EAGER) may differ from what the lazy fill would give now
   bool eager_stale = false;
+  // per-voxel setTemperature calls while the device holds the newer state: applied on the device
+  // (vxg_set_temperatures_sparse) before the next step or host read, the last call per voxel wins
+  std::vector<int> pend_voxel;
+  std::vector<float> pend_temp;
+  std::vector<int> pend_slot;  // per voxel: its entry in pend_voxel, or -1
+  // externals edited, none added: only the externals table is uploaded (vxg_set_externals)
+  bool ext_dirty = false;
+  std::vector<int> ext_voxels;  // voxels holding an external, in slot order
   // per-step actuation handed to the engine (vxg_set_actuation); re-sent after topology changes
   int act_mode = 0;
   double act_amp = 0, act_freq = 0;

@@ -390,7 +390,7 @@ CVX_External& CVX_External::operator=(const CVX_External& e) {
   return *this;
 }
 void CVX_External::touch() {
-  if (owner) owner->markTables();
+  if (owner) owner->markExternals();
 }
 void CVX_External::reset() {
   dofFixed = 0;

@@ -124,6 +124,26 @@ __global__ void k_rest_length(View S) {
   S.rest[l] = 0.5 * (vx64::base_size(S, S.lvox[l], axis) + vx64::base_size(S, S.lvox[S.nl + l], axis));
 }
 
+// CVX_Voxel::setTemperature on a list of voxels (src/VX_Voxel.cpp:108-114): temperatures, then
+// the rest lengths of their links (a link shared by two listed voxels is written twice with the
+// same value, computed from both final temperatures)
+__global__ void k_temp_sparse(View S, int n, const int* idx, const float* t) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) S.temp[idx[i]] = t[i];
+}
+template <bool FP32>
+__global__ void k_rest_sparse(vx32::View V, int n, const int* idx) {
+  const View& S = V.B;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 6 * n) return;
+  int l = S.vlinks[(k % 6) * S.nv + idx[k / 6]];
+  if (l < 0) return;
+  int axis = (S.lflags[l] >> 8) & 3;
+  int vn = S.lvox[l], vp = S.lvox[S.nl + l];
+  if (FP32) V.restDelta[l] = vx32::rest_delta(V, vn, vp, axis);
+  else S.rest[l] = 0.5 * (vx64::base_size(S, vn, axis) + vx64::base_size(S, vp, axis));
+}
+
 // stateInfo reductions (Voxelyze.cpp:752-800): per element value, block partials in double
 __device__ float info_value(const View& S, int info, int i) {
   if (info == 5) return S.stress[i];
@@ -652,6 +672,10 @@ struct vxg_engine {
   double act_amp = 0, act_freq = 0;
   float* d_phase = nullptr;
   int n_phase = 0;
+  // sparse temperature edits (vxg_set_temperatures_sparse)
+  int* d_sp_idx = nullptr;
+  float* d_sp_t = nullptr;
+  int n_sp_cap = 0;
   // scratch of the body centre-of-mass reduction
   int* d_body_off = nullptr;
   double* d_body_out = nullptr;
@@ -891,6 +915,8 @@ int vxg_destroy(vxg_engine* e) {
   if (e->d_lm) cudaFree(e->d_lm);
   if (e->d_ext) cudaFree(e->d_ext);
   if (e->d_powtab) cudaFree(e->d_powtab);
+  if (e->d_sp_idx) cudaFree(e->d_sp_idx);
+  if (e->d_sp_t) cudaFree(e->d_sp_t);
   if (e->d_partials) cudaFree(e->d_partials);
   for (int i = 0; i < 4; ++i)
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -1011,6 +1037,47 @@ int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const 
       e->adj_scope = "an external fixes some but not all degrees of freedom";
   VXG_CK(cudaStreamSynchronize(e->stream));
   rebuild_view(e);
+  return VXG_OK;
+}
+
+int vxg_set_externals(vxg_engine* e, const vxg_external* ext, int n_ext) {
+  if (!e || n_ext < 0 || (n_ext && !ext)) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  vxg_external* before = e->d_ext;
+  int rc = upload_table(e, &e->d_ext, &e->n_ext, ext, n_ext);
+  if (rc) return rc;
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  e->poisson_redo = true;        // tension terms of the Poisson strain read the externals
+  if (e->d_ext != before) rebuild_view(e);  // captured graphs hold the table's address
+  return VXG_OK;
+}
+
+int vxg_set_temperatures_sparse(vxg_engine* e, int n, const int* voxels, const float* temps) {
+  if (!e || n < 0 || (n && (!voxels || !temps))) return VXG_E_ARG;
+  if (n == 0) return VXG_OK;
+  for (int i = 0; i < n; ++i)
+    if (voxels[i] < 0 || voxels[i] >= e->nv) return fail(e, VXG_E_ARG, "vxg_set_temperatures_sparse: voxel index out of range");
+  VXG_CK(cudaSetDevice(e->device));
+  if (n > e->n_sp_cap) {
+    if (e->d_sp_idx) cudaFree(e->d_sp_idx);
+    if (e->d_sp_t) cudaFree(e->d_sp_t);
+    e->d_sp_idx = nullptr;
+    e->d_sp_t = nullptr;
+    e->n_sp_cap = 0;
+    VXG_CK(cudaMalloc(&e->d_sp_idx, sizeof(int) * (size_t)n));
+    VXG_CK(cudaMalloc(&e->d_sp_t, sizeof(float) * (size_t)n));
+    e->n_sp_cap = n;
+  }
+  VXG_CK(cudaMemcpyAsync(e->d_sp_idx, voxels, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, e->stream));
+  VXG_CK(cudaMemcpyAsync(e->d_sp_t, temps, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, e->stream));
+  k_temp_sparse<<<grid_for(n), kBlock, 0, e->stream>>>(e->S, n, e->d_sp_idx, e->d_sp_t);
+  if (e->nl) {
+    if (e->precision == VXG_FP32C) k_rest_sparse<true><<<grid_for(6 * n), kBlock, 0, e->stream>>>(e->V, n, e->d_sp_idx);
+    else k_rest_sparse<false><<<grid_for(6 * n), kBlock, 0, e->stream>>>(e->V, n, e->d_sp_idx);
+  }
+  VXG_CK(cudaGetLastError());
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  if (e->precision == VXG_FP32C) e->stale64 |= 1u << VXG_F_REST_LENGTH;  // FP64 copy is now behind
   return VXG_OK;
 }
 
