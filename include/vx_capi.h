@@ -42,6 +42,12 @@ float vx_recommended_time_step(void* s);                    /* src/Voxelyze.cpp:
 void vx_reset_time(void* s);                                /* src/Voxelyze.cpp:313-321 */
 int vx_load_json(void* s, const char* path);                /* CVoxelyze::loadJSON  src/Voxelyze.cpp:61-77, 95-162 */
 int vx_save_json(void* s, const char* path);                /* CVoxelyze::saveJSON  src/Voxelyze.cpp:79-93, 164-241 */
+/* deformed mesh of the scene (one CVX_MeshRender per simulator): */
+int vx_mesh_generate(void* s);                              /* CVX_MeshRender(CVoxelyze*) / generateMesh  src/VX_MeshRender.cpp:43-138 */
+int vx_mesh_update(void* s, int coloring, int state_info);  /* updateMesh  src/VX_MeshRender.cpp:141-218 */
+int vx_mesh_counts(void* s, int* out3);                     /* vertices, quads, edges */
+int vx_mesh_read(void* s, float* vertices, int* quads, float* normals, float* colors, int* lines);
+int vx_mesh_save_obj(void* s, const char* path);            /* saveObj  src/VX_MeshRender.cpp:238-252 */
 float vx_current_time(void* s);                             /* CVoxelyze::currentTime   include/Voxelyze.h:138 */
 /* full state dumps, layouts as in oracle/facade.h: voxels d13/f5/i2, links d22/f6/i6 */
 int vx_get_voxel_state(void* s, double* d13, float* f5, int* i2);

@@ -160,6 +160,16 @@ int vxg_set_externals(vxg_engine* e, const vxg_external* ext, int n_ext);
 /* CVX_Voxel::setTemperature (src/VX_Voxel.cpp:108-114) for n voxels at once, on the device: their
  * temperatures, then the rest lengths of their links.  Indices must be distinct. */
 int vxg_set_temperatures_sparse(vxg_engine* e, int n, const int* voxels, const float* temps);
+/* Deformed mesh of CVX_MeshRender (src/VX_MeshRender.cpp:49-218).  vxg_mesh_topology uploads the
+ * mesh: for each vertex the 8 voxels whose corner j it is (vertex_voxels[8 i + j], -1 for none, at
+ * least one per vertex) and 4 vertex indices per quad.  vxg_mesh_update computes on the device, from
+ * the current state, each vertex as the average of those voxels' corner positions
+ * (CVX_Voxel::cornerPosition, src/VX_Voxel.cpp:141-159) and each quad's unit normal, and copies
+ * them to vertices (3 floats per vertex) and normals (3 per quad) when those are not NULL.  The
+ * device copies stay readable through vxg_mesh_device_buffers (valid until the next topology). */
+int vxg_mesh_topology(vxg_engine* e, int n_vertices, const int* vertex_voxels, int n_quads, const int* quads);
+int vxg_mesh_update(vxg_engine* e, float* vertices, float* normals);
+int vxg_mesh_device_buffers(vxg_engine* e, const float** vertices, const float** normals);
 /* Tabulated powf(x, exponent) for every float x in [0.5, 2): 2^24 entries indexed by
  * (bits(x) - bits(0.5f)), computed on the host by the C library the reference links. */
 int vxg_set_powf_table(vxg_engine* e, int slot, float exponent, const float* table);

@@ -19,7 +19,7 @@ fi
 mkdir -p "$OUT"
 SRCS=""
 for f in Voxelyze VX_Voxel VX_External VX_Link VX_Material VX_MaterialVoxel VX_MaterialLink \
-         VX_Collision VX_LinearSolver; do
+         VX_Collision VX_LinearSolver VX_MeshRender; do
   SRCS="$SRCS $REF/src/$f.cpp"
 done
 FLAGS="-O3 -std=c++11 -ffp-contract=off -fPIC -shared -w -I$REF/include -I$HERE"

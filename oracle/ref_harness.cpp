@@ -5,6 +5,7 @@
 // Python tests can push a scene into the reference exactly as into the oracle or the product and
 // read back the full state.  It only calls the reference's public API; the state dump needs the
 // private members, which is why the access specifiers are opened for this translation unit.
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <vector>
@@ -18,6 +19,7 @@
 #include "VX_MaterialLink.h"
 #include "VX_MaterialVoxel.h"
 #include "VX_Voxel.h"
+#include "VX_MeshRender.h"
 #undef private
 #undef protected
 
@@ -27,7 +29,9 @@ namespace {
 struct RefSim {
   CVoxelyze vx;
   std::vector<CVX_Material*> mats;
+  CVX_MeshRender* mesh = nullptr;
   explicit RefSim(double s) : vx(s) {}
+  ~RefSim() { delete mesh; }
 };
 RefSim* S(void* s) { return static_cast<RefSim*>(s); }
 int index_of(RefSim* r, CVX_Voxel* p) {
@@ -167,7 +171,53 @@ int vxr_voxel_set_temperature(void* s, int v, float t) {
 }
 
 int vxr_do_time_step(void* s, float dt) { return S(s)->vx.doTimeStep(dt) ? 1 : 0; }
-int vxr_load_json(void* s, const char* path) { return S(s)->vx.loadJSON(path) ? 1 : 0; }
+int vxr_load_json(void* s, const char* path) {
+  RefSim* r = S(s);
+  delete r->mesh;
+  r->mesh = nullptr;
+  bool ok = r->vx.loadJSON(path);
+  r->mats.clear();
+  for (int i = 0; i < r->vx.materialCount(); ++i) r->mats.push_back(r->vx.material(i));
+  return ok ? 1 : 0;
+}
+// the reference's CVX_MeshRender (src/VX_MeshRender.cpp), same entry points as the product's vx_mesh_*
+int vxr_mesh_generate(void* s) {
+  RefSim* r = S(s);
+  if (!r->mesh) r->mesh = new CVX_MeshRender(&r->vx);
+  else r->mesh->generateMesh();
+  return 0;
+}
+int vxr_mesh_update(void* s, int coloring, int state_info) {
+  RefSim* r = S(s);
+  if (!r->mesh) return -1;
+  r->mesh->updateMesh((CVX_MeshRender::viewColoring)coloring, (CVoxelyze::stateInfoType)state_info);
+  return 0;
+}
+int vxr_mesh_counts(void* s, int* out3) {
+  RefSim* r = S(s);
+  if (!r->mesh) return -1;
+  out3[0] = (int)r->mesh->vertices.size() / 3;
+  out3[1] = (int)r->mesh->quads.size() / 4;
+  out3[2] = (int)r->mesh->lines.size() / 2;
+  return 0;
+}
+int vxr_mesh_read(void* s, float* vertices, int* quads, float* normals, float* colors, int* lines) {
+  RefSim* r = S(s);
+  if (!r->mesh) return -1;
+  CVX_MeshRender& m = *r->mesh;
+  if (vertices) std::copy(m.vertices.begin(), m.vertices.end(), vertices);
+  if (quads) std::copy(m.quads.begin(), m.quads.end(), quads);
+  if (normals) std::copy(m.quadNormals.begin(), m.quadNormals.end(), normals);
+  if (colors) std::copy(m.quadColors.begin(), m.quadColors.end(), colors);
+  if (lines) std::copy(m.lines.begin(), m.lines.end(), lines);
+  return 0;
+}
+int vxr_mesh_save_obj(void* s, const char* path) {
+  RefSim* r = S(s);
+  if (!r->mesh) return -1;
+  r->mesh->saveObj(path);
+  return 0;
+}
 int vxr_save_json(void* s, const char* path) { return S(s)->vx.saveJSON(path) ? 1 : 0; }
 int vxr_do_time_steps(void* s, int n, float dt) {
   for (int i = 0; i < n; ++i)

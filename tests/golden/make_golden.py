@@ -1,7 +1,7 @@
 """Generates the golden fixtures in this directory from the REFERENCE library compiled from its own
 sources (oracle/build_ref.sh -> oracle/_ref/libvxref.so).  Run here, where the reference tree
 exists:  python tests/golden/make_golden.py        (all fixtures)
-         python tests/golden/make_golden.py json   (the scene file only)
+         python tests/golden/make_golden.py json   (the scene file and mesh only)
 
 Each fixture holds the reference's full state after a known number of steps of one scene, either
 in full (small scenes) or as SHA-256 digests of the state bytes plus a sample of voxels (larger
@@ -62,10 +62,35 @@ def save_scene_json(lib):
     assert sim.save_json(os.path.join(HERE, "scene_ref.vxl.json"))
 
 
+def save_mesh(lib):
+    """mesh_ref.npz: the reference CVX_MeshRender of test_mesh.heated_scene with test_mesh.heat
+    applied: vertices, normals, quads, edges, the quad colours of each colouring, the OBJ text."""
+    from test_mesh import heat, heated_scene
+
+    sc = heated_scene()
+    sim = F.Sim(lib, "vxr", sc.voxel_size)
+    S.apply(sc, sim)
+    heat(sim, sim.voxel_count())
+    sim.mesh_generate()
+    out = {}
+    for coloring in (F.MESH_MATERIAL, F.MESH_FAILURE, F.MESH_STATE_INFO):
+        sim.mesh_update(coloring, F.DISPLACEMENT if coloring != F.MESH_STATE_INFO else F.KINETIC_ENERGY)
+        out[f"colors{coloring}"] = sim.mesh()["colors"]
+    m = sim.mesh()
+    for k in ("vertices", "normals", "quads", "lines"):
+        out[k] = m[k]
+    obj = os.path.join(HERE, "_mesh.obj")
+    sim.mesh_save_obj(obj)
+    out["obj"] = np.array(open(obj).read())
+    os.remove(obj)
+    np.savez_compressed(os.path.join(HERE, "mesh_ref.npz"), **out)
+
+
 def main():
     lib = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libvxref.so"))
     save_scene_json(lib)
-    if sys.argv[1:] == ["json"]:
+    save_mesh(lib)
+    if sys.argv[1:] in (["json"], ["mesh"]):
         return
     meta = {"platform": platform.machine(), "libc": platform.libc_ver()[1], "scenes": {}}
     for name, (mk, steps, cps, mode, full) in SCENES.items():

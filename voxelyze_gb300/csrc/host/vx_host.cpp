@@ -9,6 +9,7 @@
 // (resetTime, setTemperature on one voxel, topology edits) run on the mirror with the reference's
 // semantics; the time step itself never runs on the host.
 #include <algorithm>
+#include <memory>
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -16,6 +17,7 @@
 #include <thread>
 #include <unordered_set>
 
+#include "VX_MeshRender.h"
 #include "Voxelyze.h"
 #include "vx_host.h"
 #include "vxg.h"
@@ -1165,6 +1167,7 @@ namespace {
 struct Handle {
   CVoxelyze vx;
   std::vector<CVX_Material*> mats;
+  std::unique_ptr<CVX_MeshRender> mesh;
   explicit Handle(double s) : vx(s) {}
 };
 Handle* H(void* s) { return static_cast<Handle*>(s); }
@@ -1294,7 +1297,51 @@ int vx_do_time_step(void* s, float dt) {
 int vx_do_time_steps(void* s, int n, float dt) { return H(s)->vx.doTimeSteps(n, dt); }
 float vx_recommended_time_step(void* s) { return H(s)->vx.recommendedTimeStep(); }
 void vx_reset_time(void* s) { H(s)->vx.resetTime(); }
-int vx_load_json(void* s, const char* path) { return H(s)->vx.loadJSON(path) ? 1 : 0; }
+int vx_load_json(void* s, const char* path) {
+  Handle* h = H(s);
+  h->mesh.reset();
+  bool ok = h->vx.loadJSON(path);
+  h->mats.clear();  // material handles index the scene's materials
+  for (int i = 0; i < h->vx.materialCount(); ++i) h->mats.push_back(h->vx.material(i));
+  return ok ? 1 : 0;
+}
+int vx_mesh_generate(void* s) {
+  Handle* h = H(s);
+  if (!h->mesh) h->mesh.reset(new CVX_MeshRender(&h->vx));
+  else h->mesh->generateMesh();
+  return h->mesh->ok() ? 0 : -1;
+}
+int vx_mesh_update(void* s, int coloring, int state_info) {
+  Handle* h = H(s);
+  if (!h->mesh || coloring < 0 || coloring > 2 || state_info < 0 || state_info > 9) return -1;
+  h->mesh->updateMesh((CVX_MeshRender::viewColoring)coloring, (CVoxelyze::stateInfoType)state_info);
+  return h->mesh->ok() ? 0 : -1;
+}
+int vx_mesh_counts(void* s, int* out3) {
+  Handle* h = H(s);
+  if (!h->mesh || !out3) return -1;
+  out3[0] = (int)h->mesh->vertexPositions().size() / 3;
+  out3[1] = (int)h->mesh->quadVertices().size() / 4;
+  out3[2] = (int)h->mesh->lineVertices().size() / 2;
+  return 0;
+}
+int vx_mesh_read(void* s, float* vertices, int* quads, float* normals, float* colors, int* lines) {
+  Handle* h = H(s);
+  if (!h->mesh) return -1;
+  const CVX_MeshRender& m = *h->mesh;
+  if (vertices) std::copy(m.vertexPositions().begin(), m.vertexPositions().end(), vertices);
+  if (quads) std::copy(m.quadVertices().begin(), m.quadVertices().end(), quads);
+  if (normals) std::copy(m.quadNormalValues().begin(), m.quadNormalValues().end(), normals);
+  if (colors) std::copy(m.quadColorValues().begin(), m.quadColorValues().end(), colors);
+  if (lines) std::copy(m.lineVertices().begin(), m.lineVertices().end(), lines);
+  return 0;
+}
+int vx_mesh_save_obj(void* s, const char* path) {
+  Handle* h = H(s);
+  if (!h->mesh) return -1;
+  h->mesh->saveObj(path);
+  return 0;
+}
 int vx_save_json(void* s, const char* path) { return H(s)->vx.saveJSON(path) ? 1 : 0; }
 float vx_current_time(void* s) { return H(s)->vx.currentTime(); }
 

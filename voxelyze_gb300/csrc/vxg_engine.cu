@@ -144,6 +144,97 @@ __global__ void k_rest_sparse(vx32::View V, int n, const int* idx) {
   else S.rest[l] = 0.5 * (vx64::base_size(S, vn, axis) + vx64::base_size(S, vp, axis));
 }
 
+// ---- deformed mesh: CVX_MeshRender::updateMesh geometry (src/VX_MeshRender.cpp:141-180) -------
+// Position and orientation of voxel v in double: the FP64 state, or the FP32C state converted as a
+// host read converts it.
+__device__ __forceinline__ void mesh_pose(const View& S, const vx32::View& V, bool fp32, double s, int v,
+                                          double p[3], double q[4]) {
+  const int nv = S.nv;
+  if (!fp32) {
+    for (int k = 0; k < 3; ++k) p[k] = S.pos[k * nv + v];
+    for (int k = 0; k < 4; ++k) q[k] = S.orient[k * nv + v];
+    return;
+  }
+  const float4 d = V.P[v], o = V.Q[v];
+  const float dd[3] = {d.x, d.y, d.z}, oo[4] = {o.x, o.y, o.z, o.w};
+  for (int k = 0; k < 3; ++k) p[k] = S.vidx[k * nv + v] * s + ((double)dd[k] - (double)V.c[k * nv + v]);
+  for (int k = 0; k < 4; ++k) q[k] = (double)oo[k] - (double)V.qc[k * nv + v];
+}
+// CVX_Voxel::cornerPosition (src/VX_Voxel.cpp:141-159): the corner offset from the half base size
+// scaled by each axis' half-link strain (double, returned as float), rotated by the orientation
+// with the float-vector quaternion rotation (Quat3D.h:179-186), added to the float position
+__device__ void mesh_corner(const View& S, int v, int corner, const double p[3], const double q[4], float out[3]) {
+  const int nv = S.nv;
+  const vxg_voxel_material& m = S.vm[S.vmat[v]];
+  const float f = 1 + S.temp[v] * m.alphaCTE;
+  float off[3];
+  for (int i = 0; i < 3; ++i) {
+    const bool pos = corner & (1 << (2 - i));
+    const int l = S.vlinks[(2 * i + (pos ? 0 : 1)) * nv + v];
+    double st = pos ? 1.0 : -1.0;
+    if (l >= 0) {
+      const vxg_link_material& lm = S.lm[S.lmat[l]];
+      const bool failed = lm.epsilonFail != -1.0f && S.maxStrain[l] > lm.epsilonFail;
+      if (!failed) {
+        const float s0 = S.strain[l], r = S.strainRatio[l];
+        const float half = pos ? 2.0f * s0 * r / (1.0f + r) : 2.0f * s0 / (1.0f + r);  // CVX_Link::axialStrain(bool)
+        st = (double)((1 + half) * (float)(pos ? 1 : -1));
+      }
+    }
+    off[i] = (float)((0.5 * ((double)f * m.size[i])) * st);
+  }
+  const double w = q[0], x = q[1], y = q[2], z = q[3];
+  const float fx = off[0], fy = off[1], fz = off[2];
+  const float tw = (float)(fx * x + fy * y + fz * z);
+  const float tx = (float)(fx * w - fy * z + fz * y);
+  const float ty = (float)(fx * z + fy * w - fz * x);
+  const float tz = (float)(-fx * y + fy * x + fz * w);
+  out[0] = (float)p[0] + (float)(w * tx + x * tw + y * tz - z * ty);
+  out[1] = (float)p[1] + (float)(w * ty - x * tz + y * tw + z * tx);
+  out[2] = (float)p[2] + (float)(w * tz + x * ty - y * tx + z * tw);
+}
+// one mesh vertex: the average of the corner positions of the up to 8 voxels sharing it
+// (vertex_voxels[8 i + j] is the voxel whose corner j the vertex is, or -1)
+__global__ void k_mesh_vertices(View S, vx32::View V, int fp32, double s, int nvert, const int* vertex_voxels,
+                                float* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvert) return;
+  float a[3] = {0.0f, 0.0f, 0.0f};
+  int n = 0;
+  for (int j = 0; j < 8; ++j) {
+    const int v = vertex_voxels[8 * i + j];
+    if (v < 0) continue;
+    double p[3], q[4];
+    mesh_pose(S, V, fp32 != 0, s, v, p, q);
+    float c[3];
+    mesh_corner(S, v, j, p, q, c);
+    a[0] += c[0]; a[1] += c[1]; a[2] += c[2];
+    ++n;
+  }
+  const float inv = 1.0f / (float)n;  // Vec3D::operator/= multiplies by the reciprocal
+  out[3 * i] = a[0] * inv;
+  out[3 * i + 1] = a[1] * inv;
+  out[3 * i + 2] = a[2] * inv;
+}
+// quad normals: (v1 - v0) x (v3 - v0), normalised (float)
+__global__ void k_mesh_normals(int nquad, const int* quads, const float* vert, float* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nquad) return;
+  float v[4][3];
+  for (int j = 0; j < 4; ++j)
+    for (int k = 0; k < 3; ++k) v[j][k] = vert[3 * quads[4 * i + j] + k];
+  const float a0 = v[1][0] - v[0][0], a1 = v[1][1] - v[0][1], a2 = v[1][2] - v[0][2];
+  const float b0 = v[3][0] - v[0][0], b1 = v[3][1] - v[0][1], b2 = v[3][2] - v[0][2];
+  float n0 = a1 * b2 - a2 * b1, n1 = a2 * b0 - a0 * b2, n2 = a0 * b1 - a1 * b0;
+  const float l = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+  if (l > 0) {  // Vec3D::Normalize divides each component
+    n0 /= l; n1 /= l; n2 /= l;
+  }
+  out[3 * i] = n0;
+  out[3 * i + 1] = n1;
+  out[3 * i + 2] = n2;
+}
+
 // stateInfo reductions (Voxelyze.cpp:752-800): per element value, block partials in double
 __device__ float info_value(const View& S, int info, int i) {
   if (info == 5) return S.stress[i];
@@ -672,6 +763,12 @@ struct vxg_engine {
   double act_amp = 0, act_freq = 0;
   float* d_phase = nullptr;
   int n_phase = 0;
+  // deformed mesh (vxg_mesh_topology / vxg_mesh_update)
+  int* d_mesh_vv = nullptr;     // 8 voxels per vertex
+  int* d_mesh_quads = nullptr;  // 4 vertices per quad
+  float* d_mesh_vert = nullptr;
+  float* d_mesh_norm = nullptr;
+  int n_mesh_vert = 0, n_mesh_quad = 0;
   // sparse temperature edits (vxg_set_temperatures_sparse)
   int* d_sp_idx = nullptr;
   float* d_sp_t = nullptr;
@@ -917,6 +1014,8 @@ int vxg_destroy(vxg_engine* e) {
   if (e->d_powtab) cudaFree(e->d_powtab);
   if (e->d_sp_idx) cudaFree(e->d_sp_idx);
   if (e->d_sp_t) cudaFree(e->d_sp_t);
+  for (void* p : {(void*)e->d_mesh_vv, (void*)e->d_mesh_quads, (void*)e->d_mesh_vert, (void*)e->d_mesh_norm})
+    if (p) cudaFree(p);
   if (e->d_partials) cudaFree(e->d_partials);
   for (int i = 0; i < 4; ++i)
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -1078,6 +1177,63 @@ int vxg_set_temperatures_sparse(vxg_engine* e, int n, const int* voxels, const f
   VXG_CK(cudaGetLastError());
   VXG_CK(cudaStreamSynchronize(e->stream));
   if (e->precision == VXG_FP32C) e->stale64 |= 1u << VXG_F_REST_LENGTH;  // FP64 copy is now behind
+  return VXG_OK;
+}
+
+int vxg_mesh_topology(vxg_engine* e, int n_vertices, const int* vertex_voxels, int n_quads, const int* quads) {
+  if (!e || n_vertices < 0 || n_quads < 0 || (n_vertices && !vertex_voxels) || (n_quads && !quads)) return VXG_E_ARG;
+  for (long long i = 0; i < 8ll * n_vertices; ++i)
+    if (vertex_voxels[i] < -1 || vertex_voxels[i] >= e->nv) return fail(e, VXG_E_ARG, "vxg_mesh_topology: voxel index out of range");
+  for (long long i = 0; i < 4ll * n_quads; ++i)
+    if (quads[i] < 0 || quads[i] >= n_vertices) return fail(e, VXG_E_ARG, "vxg_mesh_topology: vertex index out of range");
+  for (int i = 0; i < n_vertices; ++i) {
+    bool any = false;
+    for (int j = 0; j < 8; ++j) any |= vertex_voxels[8 * i + j] >= 0;
+    if (!any) return fail(e, VXG_E_ARG, "vxg_mesh_topology: a vertex belongs to no voxel");
+  }
+  VXG_CK(cudaSetDevice(e->device));
+  for (void* p : {(void*)e->d_mesh_vv, (void*)e->d_mesh_quads, (void*)e->d_mesh_vert, (void*)e->d_mesh_norm})
+    if (p) cudaFree(p);
+  e->d_mesh_vv = e->d_mesh_quads = nullptr;
+  e->d_mesh_vert = e->d_mesh_norm = nullptr;
+  e->n_mesh_vert = e->n_mesh_quad = 0;
+  VXG_CK(cudaMalloc(&e->d_mesh_vv, sizeof(int) * 8 * (size_t)std::max(n_vertices, 1)));
+  VXG_CK(cudaMalloc(&e->d_mesh_vert, sizeof(float) * 3 * (size_t)std::max(n_vertices, 1)));
+  VXG_CK(cudaMalloc(&e->d_mesh_quads, sizeof(int) * 4 * (size_t)std::max(n_quads, 1)));
+  VXG_CK(cudaMalloc(&e->d_mesh_norm, sizeof(float) * 3 * (size_t)std::max(n_quads, 1)));
+  if (n_vertices)
+    VXG_CK(cudaMemcpyAsync(e->d_mesh_vv, vertex_voxels, sizeof(int) * 8 * (size_t)n_vertices, cudaMemcpyHostToDevice, e->stream));
+  if (n_quads)
+    VXG_CK(cudaMemcpyAsync(e->d_mesh_quads, quads, sizeof(int) * 4 * (size_t)n_quads, cudaMemcpyHostToDevice, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  e->n_mesh_vert = n_vertices;
+  e->n_mesh_quad = n_quads;
+  return VXG_OK;
+}
+
+int vxg_mesh_update(vxg_engine* e, float* vertices, float* normals) {
+  if (!e) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  ensure32(e);  // FP32C: host-written state first
+  const int nvt = e->n_mesh_vert, nq = e->n_mesh_quad;
+  if (nvt) {
+    k_mesh_vertices<<<grid_for(nvt), kBlock, 0, e->stream>>>(e->S, e->V, e->precision == VXG_FP32C ? 1 : 0,
+                                                            e->g.voxSize, nvt, e->d_mesh_vv, e->d_mesh_vert);
+    if (nq) k_mesh_normals<<<grid_for(nq), kBlock, 0, e->stream>>>(nq, e->d_mesh_quads, e->d_mesh_vert, e->d_mesh_norm);
+    VXG_CK(cudaGetLastError());
+    if (vertices)
+      VXG_CK(cudaMemcpyAsync(vertices, e->d_mesh_vert, sizeof(float) * 3 * (size_t)nvt, cudaMemcpyDeviceToHost, e->stream));
+    if (normals && nq)
+      VXG_CK(cudaMemcpyAsync(normals, e->d_mesh_norm, sizeof(float) * 3 * (size_t)nq, cudaMemcpyDeviceToHost, e->stream));
+  }
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  return VXG_OK;
+}
+
+int vxg_mesh_device_buffers(vxg_engine* e, const float** vertices, const float** normals) {
+  if (!e) return VXG_E_ARG;
+  if (vertices) *vertices = e->d_mesh_vert;
+  if (normals) *normals = e->d_mesh_norm;
   return VXG_OK;
 }
 

@@ -77,7 +77,15 @@ _SIGS = {
 _OPT_SIGS = {
     "load_json": (_i, [_p, C.c_char_p]),
     "save_json": (_i, [_p, C.c_char_p]),
+    "mesh_generate": (_i, [_p]),
+    "mesh_update": (_i, [_p, _i, _i]),
+    "mesh_counts": (_i, [_p, _ip]),
+    "mesh_read": (_i, [_p, _fp, _ip, _fp, _fp, _ip]),
+    "mesh_save_obj": (_i, [_p, C.c_char_p]),
 }
+
+# CVX_MeshRender::viewColoring
+MESH_MATERIAL, MESH_FAILURE, MESH_STATE_INFO = 0, 1, 2
 
 
 def bind(lib: C.CDLL, prefix: str) -> dict:
@@ -218,6 +226,30 @@ class Sim:
 
     def save_json(self, path: str) -> bool:
         return self.f["save_json"](self.h, path.encode()) == 1
+
+    # -- deformed mesh (CVX_MeshRender) -----------------------------------------------------
+    def mesh_generate(self) -> bool:
+        """Builds (or rebuilds) the mesh and updates it once; False if the update could not run."""
+        return self.f["mesh_generate"](self.h) == 0
+
+    def mesh_update(self, coloring: int = 0, state_info: int = 0) -> bool:
+        return self.f["mesh_update"](self.h, coloring, state_info) == 0
+
+    def mesh(self) -> dict:
+        n = np.zeros(3, np.int32)
+        if self.f["mesh_counts"](self.h, _ptr(n, C.c_int)) != 0:
+            raise RuntimeError("no mesh: call mesh_generate first")
+        nv, nq, nl = (int(x) for x in n)
+        out = {"vertices": np.zeros((nv, 3), np.float32), "quads": np.zeros((nq, 4), np.int32),
+               "normals": np.zeros((nq, 3), np.float32), "colors": np.zeros((nq, 3), np.float32),
+               "lines": np.zeros((nl, 2), np.int32)}
+        self.f["mesh_read"](self.h, _ptr(out["vertices"], C.c_float), _ptr(out["quads"], C.c_int),
+                            _ptr(out["normals"], C.c_float), _ptr(out["colors"], C.c_float),
+                            _ptr(out["lines"], C.c_int))
+        return out
+
+    def mesh_save_obj(self, path: str) -> bool:
+        return self.f["mesh_save_obj"](self.h, path.encode()) == 0
 
     def current_time(self) -> float:
         return self.f["current_time"](self.h)
