@@ -211,3 +211,24 @@ def test_collisions_fp32c_tracks_fp64(product_lib, friction):
         assert rel_pos <= 1e-3
     else:
         assert rel_pos <= 1e-5
+
+
+def test_positions_into_pinned_memory(product_lib):
+    """Reading FP32C positions into pinned host memory converts them on the device straight into
+    that buffer; the values equal the staged read (pageable destination) bit for bit."""
+    import ctypes as C
+
+    import torch
+
+    sc = S.lattice(24, 20, 10)
+    s = _fp32c(product_lib, sc, 0)
+    dt = s.recommended_time_step()
+    read = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)(("vx_read_positions", product_lib))
+    for _ in range(3):
+        assert s.do_time_steps(25, dt) == 25
+        pinned = torch.empty(3 * s.voxel_count(), dtype=torch.float64, pin_memory=True)
+        assert read(s.h, pinned.data_ptr()) == 0
+        staged = np.zeros(3 * s.voxel_count(), np.float64)
+        assert read(s.h, staged.ctypes.data) == 0
+        assert np.array_equal(pinned.numpy(), staged)
+        assert np.array_equal(staged.reshape(3, -1).T, s.voxel_state()["pos"])

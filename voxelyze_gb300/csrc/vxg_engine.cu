@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -600,6 +601,19 @@ __global__ void k_conv(vx32::View S, double s, int field, int to32) {
     default: break;
   }
 }
+// FP32C positions converted straight into a destination the device can write (pinned host memory
+// reached over the host link, or device memory): the same conversion as k_conv, no staging copy
+__global__ void k_pos_out(vx32::View S, double s, double* dst) {
+  const vx64::View& B = S.B;
+  const int nv = B.nv;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const float4 d = S.P[i];
+  const float dd[3] = {d.x, d.y, d.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) dst[k * nv + i] = B.vidx[k * nv + i] * s + ((double)dd[k] - (double)S.c[k * nv + i]);
+}
+
 // Per-step actuation: before each step's link pass every voxel's temperature is set to
 //   amplitude * sin(2 pi frequency t + phase)      (t = CVoxelyze::currentTime at the step start)
 // and every rest length follows, i.e. the reference's setAmbientTemperature(T, true) (mode 1, one
@@ -756,6 +770,7 @@ struct vxg_engine {
   // the last step makes the next batch refill those caches first (k_poisson<true>)
   bool poisson_redo = true;
   bool poisson_fuse = true;  // vxg_set_poisson_fusion
+  int* h_ctl = nullptr;      // pinned copy of the batch's control words
   // kernels launched by the time step (a graph replay counts the kernels it holds)
   long long n_launch = 0, graph_kernels = 0, cgraph_kernels = 0;
   // per-step actuation (vxg_set_actuation)
@@ -1021,6 +1036,7 @@ int vxg_destroy(vxg_engine* e) {
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);
   for (cudaEvent_t x : e->tev) cudaEventDestroy(x);
   for (cudaEvent_t x : e->bev) if (x) cudaEventDestroy(x);
+  if (e->h_ctl) cudaFreeHost(e->h_ctl);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return VXG_OK;
@@ -1107,6 +1123,18 @@ int vxg_get_field(vxg_engine* e, int f, void* host, long long count) {
   long long n = (long long)d.comps * (d.per_link ? e->nl : e->nv);
   if (count != n) return fail(e, VXG_E_SIZE, "vxg_get_field: element count mismatch");
   if (n == 0) return VXG_OK;
+  if (f == VXG_F_POS && e->precision == VXG_FP32C && (e->stale64 & (1u << VXG_F_POS))) {
+    // positions the device can write directly (pinned host memory): convert into them in one pass
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+      ensure32(e);
+      k_pos_out<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->V, e->g.voxSize, (double*)pa.devicePointer);
+      VXG_CK(cudaGetLastError());
+      VXG_CK(cudaStreamSynchronize(e->stream));
+      return VXG_OK;
+    }
+    cudaGetLastError();  // not a registered pointer: the staged path below
+  }
   if (is_state_field(f)) ensure64(e, f);
   VXG_CK(cudaMemcpyAsync(host, e->field_ptr[f], (size_t)n * d.elem, cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
@@ -1313,8 +1341,9 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   const int gl = grid_of(e->nl, bl), gv = grid_of(e->nv, bv);
   if (ev) cudaEventRecord(ev[0], e->stream);
   // kernels this step launches (or, under capture, records)
+  (void)first;
   long long nk = 1 + (e->nl ? 1 : 0) + (e->act_mode && e->nv ? 1 + (e->nl ? 1 : 0) : 0) +
-                 (e->g.any_poisson && e->nv && (first || !fused_poisson(e)) ? 1 : 0);
+                 (e->g.any_poisson && e->nv && !fused_poisson(e) ? 1 : 0);
   if (e->act_mode && e->nv) {
     k_actuate<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S, e->act_amp, e->act_freq, e->act_mode == 2 ? e->d_phase : nullptr,
                                                         e->precision == VXG_FP32C ? 1 : 0);
@@ -1323,9 +1352,9 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
       else k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(S);
     }
   }
-  // FP32C fills the cache in the voxel pass; its pre-pass runs once per batch (for caches the host
-  // invalidated) and then finds nothing to do
-  if (e->g.any_poisson && e->nv && (first || !fused_poisson(e)))
+  // FP32C fills the cache in the voxel pass; caches the host invalidated are refilled before the
+  // batch (poisson_refill), so no pre-pass runs inside it
+  if (e->g.any_poisson && e->nv && !fused_poisson(e))
     k_poisson<false><<<grid_for(e->nv), kBlock, 0, e->stream>>>(S);
   if (e->precision == VXG_FP32C) {
     if (e->nl) {
@@ -1400,11 +1429,11 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   VXG_CK(cudaSetDevice(e->device));
   ensure32(e);
   if (e->precision == VXG_FP32C) e->stale64 = all_state_bits();
-  // reset the per-batch control words (keep time and counters)
-  int zeros[4] = {0, 0, 0, 0};
-  VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
-  unsigned z2[2] = {0u, 0u};
-  VXG_CK(cudaMemcpyAsync(e->ctl->maxf, z2, sizeof(z2), cudaMemcpyHostToDevice, e->stream));
+  // reset the per-batch control words: diverged, halt, steps, status and the dt maxima (keep time
+  // and counters)
+  static_assert(offsetof(Ctl, maxf) == 4 * sizeof(int) && offsetof(Ctl, time) == 4 * sizeof(int) + 2 * sizeof(unsigned),
+                "control block layout");
+  VXG_CK(cudaMemsetAsync(e->ctl, 0, offsetof(Ctl, time), e->stream));
   poisson_refill(e);
   bool use_graph = e->timing != 1 && nsteps > 1;
   if (e->timing == 2) {
@@ -1455,9 +1484,10 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
     for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == 0);
   }
   if (e->timing == 2) VXG_CK(cudaEventRecord(e->bev[1], e->stream));
-  int h[4];
-  VXG_CK(cudaMemcpyAsync(h, e->ctl, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+  if (!e->h_ctl) VXG_CK(cudaMallocHost(&e->h_ctl, 4 * sizeof(int)));
+  VXG_CK(cudaMemcpyAsync(e->h_ctl, e->ctl, 4 * sizeof(int), cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
+  const int* h = e->h_ctl;
   VXG_CK(cudaGetLastError());
   if (e->timing == 2) VXG_CK(cudaEventElapsedTime(&e->t_batch, e->bev[0], e->bev[1]));
   if (e->timing == 1 && e->tev_used > 0) {
