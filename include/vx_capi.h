@@ -20,6 +20,10 @@ int vx_material_set_model_bilinear(void* s, int mat, float E, float plastic_E, f
                                    float fail_stress);                            /* src/VX_Material.cpp:389-434 */
 int vx_material_set_model(void* s, int mat, int n, const float* strain, const float* stress); /* :283-350 */
 int vx_set_voxel(void* s, int mat, int x, int y, int z);    /* setVoxel                 src/Voxelyze.cpp:422-437 */
+int vx_remove_voxel(void* s, int x, int y, int z);          /* setVoxel(NULL, ...)      src/Voxelyze.cpp:424-427, 464-483 */
+int vx_replace_material(void* s, int a, int b);             /* replaceMaterial          src/Voxelyze.cpp:406-420 */
+int vx_remove_material(void* s, int m);                     /* removeMaterial           src/Voxelyze.cpp:384-404 */
+void vx_set_voxel_size(void* s, double size);               /* setVoxelSize             src/Voxelyze.cpp:643-668 */
 int vx_set_voxels(void* s, int n, const int* mat, const int* xyz); /* n setVoxel calls in order */
 int vx_voxel_count(void* s);                                /* voxelCount               include/Voxelyze.h:98 */
 int vx_link_count(void* s);                                 /* linkCount                include/Voxelyze.h:111 */

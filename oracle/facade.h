@@ -27,6 +27,10 @@ extern "C" {
   int P##_material_set_model(void* s, int mat, int n, const float* strain, const float* stress);    \
   int P##_set_voxel(void* s, int mat, int x, int y, int z);                                         \
   int P##_set_voxels(void* s, int n, const int* mat, const int* xyz);                               \
+  int P##_remove_voxel(void* s, int x, int y, int z);                                               \
+  int P##_replace_material(void* s, int a, int b);                                                  \
+  int P##_remove_material(void* s, int m);                                                          \
+  void P##_set_voxel_size(void* s, double size);                                                    \
   int P##_voxel_count(void* s);                                                                     \
   int P##_link_count(void* s);                                                                      \
   int P##_voxel_index(void* s, int x, int y, int z);                                                \

@@ -98,6 +98,23 @@ int vxr_set_voxel(void* s, int mat, int x, int y, int z) {
   CVX_Material* m = (mat >= 0 && mat < (int)r->mats.size()) ? r->mats[mat] : nullptr;
   return index_of(r, r->vx.setVoxel(m, x, y, z));
 }
+int vxr_remove_voxel(void* s, int x, int y, int z) {
+  S(s)->vx.setVoxel(nullptr, x, y, z);
+  return 0;
+}
+int vxr_replace_material(void* s, int a, int b) {
+  RefSim* r = S(s);
+  if (a < 0 || b < 0 || a >= (int)r->mats.size() || b >= (int)r->mats.size()) return -1;
+  return r->vx.replaceMaterial(r->mats[a], r->mats[b]) ? 0 : -1;
+}
+int vxr_remove_material(void* s, int m) {
+  RefSim* r = S(s);
+  if (m < 0 || m >= (int)r->mats.size()) return -1;
+  if (!r->vx.removeMaterial(r->mats[m])) return -1;
+  r->mats.erase(r->mats.begin() + m);
+  return 0;
+}
+void vxr_set_voxel_size(void* s, double size) { S(s)->vx.setVoxelSize(size); }
 int vxr_set_voxels(void* s, int n, const int* mat, const int* xyz) {
   RefSim* r = S(s);
   for (int i = 0; i < n; ++i) {

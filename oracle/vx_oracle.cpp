@@ -1031,6 +1031,135 @@ struct Sim {
     return idx;
   }
 
+  // ---- topology edits (Voxelyze.cpp:384-498, 541-575, 643-668) ---------------------------
+  // CVoxelyze::removeLink: the link leaves the list (later links move down one index) and both end
+  // voxels lose it (surface flags updated)
+  void remove_link(int x, int y, int z, int dir) {
+    int ax = dir / 2;
+    auto it = lmap[ax].find(Key{x - (dir == 1), y - (dir == 3), z - (dir == 5)});
+    if (it == lmap[ax].end()) return;
+    const int li = it->second;
+    lmap[ax].erase(it);
+    links.erase(links.begin() + li);
+    for (auto& m : lmap)
+      for (auto& kv : m)
+        if (kv.second > li) kv.second--;
+    for (Voxel& v : voxels)
+      for (int& sl : v.links) {
+        if (sl == li) sl = -1;
+        else if (sl > li) sl--;
+      }
+    int v1 = voxel_at(x, y, z);
+    if (v1 >= 0) update_surface(voxels[v1]);
+    const int* o = dir_off(dir);
+    int v2 = voxel_at(x + o[0], y + o[1], z + o[2]);
+    if (v2 >= 0) update_surface(voxels[v2]);
+  }
+  // CVoxelyze::removeVoxel: the voxel leaves the list (later voxels move down one index) with its
+  // links
+  void remove_voxel(int x, int y, int z) {
+    nearbyStale = collisionsStale = true;
+    const int v = voxel_at(x, y, z);
+    if (v < 0) return;
+    vmap.erase(Key{x, y, z});
+    for (int d = 0; d < 6; ++d) remove_link(x, y, z, d);
+    voxels.erase(voxels.begin() + v);
+    for (auto& kv : vmap)
+      if (kv.second > v) kv.second--;
+    for (Link& l : links) {
+      if (l.vneg > v) l.vneg--;
+      if (l.vpos > v) l.vpos--;
+    }
+  }
+  // CVoxelyze::replaceVoxel with CVX_Voxel::replaceMaterial (VX_Voxel.cpp:78-90): momenta scaled to
+  // keep the velocities, static friction cleared, Poisson cache invalid, links rebuilt (they move
+  // to the end of the list)
+  void replace_voxel(int mat, int x, int y, int z) {
+    collisionsStale = true;
+    const int v = voxel_at(x, y, z);
+    Voxel& vx = voxels[v];
+    const float fm = vmats[mat].mass / vmats[vx.mat].mass;
+    const float fi = vmats[mat].inertia / vmats[vx.mat].inertia;
+    vx.linMom = v3(vx.linMom.x * fm, vx.linMom.y * fm, vx.linMom.z * fm);
+    vx.angMom = v3(vx.angMom.x * fi, vx.angMom.y * fi, vx.angMom.z * fi);
+    vx.staticFriction = false;
+    vx.pStrainInvalid = true;
+    vx.mat = mat;
+    for (int d = 0; d < 6; ++d) {
+      remove_link(x, y, z, d);
+      add_link(x, y, z, d);
+    }
+  }
+  // CVoxelyze::setVoxel (Voxelyze.cpp:422-437)
+  int set_voxel(int mat, int x, int y, int z) {
+    if (mat < 0) {
+      remove_voxel(x, y, z);
+      return -1;
+    }
+    int v = voxel_at(x, y, z);
+    if (v >= 0) {
+      replace_voxel(mat, x, y, z);
+      return v;
+    }
+    return add_voxel(mat, x, y, z);
+  }
+  // CVoxelyze::replaceMaterial: the lattice is visited z, then y, then x (the reference walks its
+  // bounding box in that order; an empty cell there dereferences a null voxel, so only occupied
+  // cells are visited here)
+  void replace_material(int a, int b) {
+    std::vector<Key> cells;
+    for (const Voxel& v : voxels)
+      if (v.mat == a) cells.push_back(Key{v.ix, v.iy, v.iz});
+    std::sort(cells.begin(), cells.end(), [](const Key& p, const Key& q) {
+      if (p.z != q.z) return p.z < q.z;
+      if (p.y != q.y) return p.y < q.y;
+      return p.x < q.x;
+    });
+    for (const Key& k : cells) set_voxel(b, k.x, k.y, k.z);
+  }
+  // CVoxelyze::removeMaterial: its voxels, then the material; the link materials built from it go
+  // too (the reference leaves them in its list, unused)
+  void remove_material(int m) {
+    std::vector<Key> cells;
+    for (const Voxel& v : voxels)
+      if (v.mat == m) cells.push_back(Key{v.ix, v.iy, v.iz});
+    for (const Key& k : cells) remove_voxel(k.x, k.y, k.z);
+    std::vector<int> lnew(lmats.size(), -1);
+    std::vector<Material> keep;
+    for (size_t i = 0; i < lmats.size(); ++i)
+      if (lmats[i].m1 != m && lmats[i].m2 != m) {
+        lnew[i] = (int)keep.size();
+        keep.push_back(lmats[i]);
+      }
+    lmats.swap(keep);
+    for (Material& L : lmats) {
+      if (L.m1 > m) L.m1--;
+      if (L.m2 > m) L.m2--;
+    }
+    for (Link& l : links) l.mat = lnew[l.mat];
+    vmats.erase(vmats.begin() + m);
+    for (Voxel& v : voxels)
+      if (v.mat > m) v.mat--;
+  }
+  // CVoxelyze::setVoxelSize: voxel materials take the new nominal size (CVX_MaterialVoxel::
+  // setNominalSize, whose derived update also refreshes the link materials built from it),
+  // positions scale, motion stops, static friction clears, links reset
+  void set_voxel_size(double s) {
+    double f = s / voxSize;
+    voxSize = s;
+    for (size_t k = 0; k < vmats.size(); ++k) {
+      vmats[k].nomSize = s <= 0 ? FLT_MIN : s;
+      voxel_material_changed((int)k);
+    }
+    for (Voxel& v : voxels) {
+      v.pos = v3(v.pos.x * f, v.pos.y * f, v.pos.z * f);
+      v.linMom = v.angMom = V3();
+      v.staticFriction = false;
+    }
+    for (Link& l : links) reset_link(l);
+    collisionsStale = true;
+  }
+
   // ---- time step (Voxelyze.cpp:251-311) --------------------------------------------------
   float recommended_dt() {
     float mx = 0.0f;
@@ -1274,11 +1403,26 @@ int vxo_material_set_model(void* s, int mat, int n, const float* strain, const f
 
 int vxo_set_voxel(void* s, int mat, int x, int y, int z) {
   Sim* r = S(s);
-  if (mat < 0 || mat >= (int)r->vmats.size()) return -1;  // removal is not restated
-  int v = r->voxel_at(x, y, z);
-  if (v >= 0) return v;  // material replacement is not restated
-  return r->add_voxel(mat, x, y, z);
+  if (mat < 0 || mat >= (int)r->vmats.size()) return -1;
+  return r->set_voxel(mat, x, y, z);
 }
+int vxo_remove_voxel(void* s, int x, int y, int z) {
+  S(s)->set_voxel(-1, x, y, z);
+  return 0;
+}
+int vxo_replace_material(void* s, int a, int b) {
+  Sim* r = S(s);
+  if (a < 0 || b < 0 || a >= (int)r->vmats.size() || b >= (int)r->vmats.size()) return -1;
+  r->replace_material(a, b);
+  return 0;
+}
+int vxo_remove_material(void* s, int m) {
+  Sim* r = S(s);
+  if (m < 0 || m >= (int)r->vmats.size()) return -1;
+  r->remove_material(m);
+  return 0;
+}
+void vxo_set_voxel_size(void* s, double size) { S(s)->set_voxel_size(size); }
 int vxo_set_voxels(void* s, int n, const int* mat, const int* xyz) {
   for (int i = 0; i < n; ++i) vxo_set_voxel(s, mat[i], xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
   return 0;

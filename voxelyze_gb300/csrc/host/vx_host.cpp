@@ -182,9 +182,16 @@ bool CVoxelyze::removeMaterial(CVX_Material* toRemove) {  // Voxelyze.cpp:384-40
 
 bool CVoxelyze::replaceMaterial(CVX_Material* a, CVX_Material* b) {  // Voxelyze.cpp:406-420
   if (!exists((CVX_MaterialVoxel*)a) || !exists((CVX_MaterialVoxel*)b)) return false;
+  // the reference walks its bounding box z, then y, then x (each replacement moves the voxel's
+  // links to the end of the link list, so the order fixes the link order); occupied cells only
   std::vector<CVX_Voxel*> hit;
   for (CVX_Voxel* v : voxelsList)
     if (v->mat == (CVX_MaterialVoxel*)a) hit.push_back(v);
+  std::sort(hit.begin(), hit.end(), [](const CVX_Voxel* p, const CVX_Voxel* q) {
+    if (p->iz != q->iz) return p->iz < q->iz;
+    if (p->iy != q->iy) return p->iy < q->iy;
+    return p->ix < q->ix;
+  });
   for (CVX_Voxel* v : hit) setVoxel(b, v->ix, v->iy, v->iz);
   return true;
 }
@@ -1228,6 +1235,23 @@ int vx_set_voxel(void* s, int mat, int x, int y, int z) {
   CVX_Voxel* v = h->vx.setVoxel(m, x, y, z);
   return v ? v->index() : -1;
 }
+int vx_remove_voxel(void* s, int x, int y, int z) {
+  H(s)->vx.setVoxel(nullptr, x, y, z);
+  return 0;
+}
+int vx_replace_material(void* s, int a, int b) {
+  Handle* h = H(s);
+  if (a < 0 || b < 0 || a >= (int)h->mats.size() || b >= (int)h->mats.size()) return -1;
+  return h->vx.replaceMaterial(h->mats[a], h->mats[b]) ? 0 : -1;
+}
+int vx_remove_material(void* s, int m) {
+  Handle* h = H(s);
+  if (m < 0 || m >= (int)h->mats.size()) return -1;
+  if (!h->vx.removeMaterial(h->mats[m])) return -1;
+  h->mats.erase(h->mats.begin() + m);
+  return 0;
+}
+void vx_set_voxel_size(void* s, double size) { H(s)->vx.setVoxelSize(size); }
 int vx_set_voxels(void* s, int n, const int* mat, const int* xyz) {
   for (int i = 0; i < n; ++i) vx_set_voxel(s, mat[i], xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
   return 0;

@@ -38,6 +38,10 @@ _dp = C.POINTER(C.c_double)
 
 _SIGS = {
     "create": (_p, [_d]),
+    "remove_voxel": (_i, [_p, _i, _i, _i]),
+    "replace_material": (_i, [_p, _i, _i]),
+    "remove_material": (_i, [_p, _i]),
+    "set_voxel_size": (None, [_p, _d]),
     "destroy": (None, [_p]),
     "add_material": (_i, [_p, _f, _f]),
     "material_set": (_i, [_p, _i, _i, _f]),
@@ -219,6 +223,20 @@ class Sim:
 
     def reset_time(self):
         self.f["reset_time"](self.h)
+
+    # -- topology edits (CVoxelyze::setVoxel(NULL), replaceMaterial, removeMaterial,
+    #    setVoxelSize) ---------------------------------------------------------------------
+    def remove_voxel(self, x: int, y: int, z: int):
+        self.f["remove_voxel"](self.h, x, y, z)
+
+    def replace_material(self, a: int, b: int) -> bool:
+        return self.f["replace_material"](self.h, a, b) == 0
+
+    def remove_material(self, m: int) -> bool:
+        return self.f["remove_material"](self.h, m) == 0
+
+    def set_voxel_size(self, size: float):
+        self.f["set_voxel_size"](self.h, size)
 
     # -- scene files (CVoxelyze::loadJSON / saveJSON) ---------------------------------------
     def load_json(self, path: str) -> bool:
