@@ -341,8 +341,9 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
     else stress = m.E * rel;
   }
   B.strain[l] = axial;
-  B.maxStrain[l] = maxStrain;
-  B.strainOffset[l] = strainOffset;
+  // the plastic history and the flags change rarely: stored only when their bits change
+  if (vx64::float_bits(maxStrain) != vx64::float_bits(in.maxStrain)) B.maxStrain[l] = maxStrain;
+  if (vx64::float_bits(strainOffset) != vx64::float_bits(in.strainOffset)) B.strainOffset[l] = strainOffset;
   B.stress[l] = stress;
 
   f3 fN, fP, mN, mP;
@@ -384,7 +385,8 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
   st3(S.fP, nl, l, fP);
   st3(S.mN, nl, l, mN);
   st3(S.mP, nl, l, mP);
-  B.lflags[l] = (lf & ~3u) | (smallAngle ? VXG_LF_SMALL_ANGLE : 0u) | (lvv ? VXG_LF_LOCAL_VEL_VALID : 0u);
+  const uint32_t nf = (lf & ~3u) | (smallAngle ? VXG_LF_SMALL_ANGLE : 0u) | (lvv ? VXG_LF_LOCAL_VEL_VALID : 0u);
+  if (nf != lf) B.lflags[l] = nf;
   return axial;
 }
 

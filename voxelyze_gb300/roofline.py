@@ -36,10 +36,12 @@ def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
 
 
 # FP32C layout (voxelyze_gb300/csrc/vx_phys32.cuh):
-#   link pass, per link : endpoint ids 8, flags 4+4, material id 4, previous pos2/angle1v/angle2v
+#   link pass, per link : endpoint ids 8, flags 4 read, material id 4, previous pos2/angle1v/angle2v
 #                         36 read + 36 written, rest offset 4, transverse area/strain sum 8 read +
-#                         8 written, strain/maxStrain/strainOffset 12 read + 16 written, forces and
-#                         moments 48 written                                              = 188 B
+#                         8 written, maxStrain/strainOffset 8 read, strain and stress 8 written,
+#                         forces and moments 48 written                                   = 176 B
+#                         (flags, maxStrain and strainOffset are written only when they change,
+#                         which is rare, so those writes are not counted)
 #             per voxel : displacement 12, orientation 16, material id 4                  =  32 B
 #                         (+ the cached Poisson strain 12 when nu != 0)
 #   voxel pass, per voxel: displacement and orientation with their compensations, momenta 80 read
@@ -48,7 +50,7 @@ def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
 #             per link  : the force and moment each end gathers, 2 x 24                   =  48 B
 #   Poisson cache (nu != 0), filled by the voxel pass for the next step: cached strain 12 B written
 #                         per voxel, strain and strain ratio 8 B per link gathered
-FP32C_LINK_PER_LINK = 188
+FP32C_LINK_PER_LINK = 176
 FP32C_LINK_PER_VOXEL = 32
 FP32C_LINK_PER_VOXEL_POISSON = 12
 FP32C_VOXEL_PER_VOXEL = 208
