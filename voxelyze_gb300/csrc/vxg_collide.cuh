@@ -4,7 +4,9 @@
 // Per step, on the engine stream:
 //   c_check    each surface voxel tests its drift from the position at the last rebuild (float
 //              copy, double distance, as the reference) and raises the device "stale" flag
-//   rebuild    only when stale (each kernel exits at once otherwise):
+//   rebuild    only when stale (it exits at once otherwise); one cooperative launch (c_rebuild)
+//              runs these phases with grid-wide barriers between them, or, where cooperative
+//              launches are not available, six separate kernels:
 //              c_insert  surface voxels into a uniform hash grid (cell = watch radius), open
 //                        addressing on the packed cell key, one linked list per cell
 //              c_count   each surface voxel counts partners within the watch radius that are not
@@ -18,6 +20,7 @@
 //   c_contact  one thread per pair: the penalty + damping contact force (float math)
 // The voxel pass subtracts each voxel's contact forces in its contact-list order.
 #pragma once
+#include <cooperative_groups.h>
 
 struct ColCtl {
   int stale;        // rebuild needed this step
@@ -108,13 +111,20 @@ __global__ void c_check(ColView C) {
   if (dx * dx + dy * dy + dz * dz > C.recalc2) C.cc->stale = 1;
 }
 
-__global__ void c_clear(ColView C) {
-  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i <= C.hcap_mask;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
+// rebuild only when c_check found the list stale and the step has not diverged (the same for
+// every thread of a launch: nothing writes these words while a rebuild kernel runs)
+__device__ __forceinline__ bool c_rebuilding(const ColView& C) {
+  return C.cc->stale && !C.ctl->halt && !C.ctl->diverged;
+}
+__device__ __forceinline__ void c_clear_range(const ColView& C, unsigned long long first, unsigned long long stride) {
+  for (unsigned long long i = first; i <= C.hcap_mask; i += stride) {
     C.hkey[i] = ~0ull;
     C.hhead[i] = -1;
   }
+}
+__global__ void c_clear(ColView C) {
+  if (!c_rebuilding(C)) return;
+  c_clear_range(C, blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x, (unsigned long long)gridDim.x * blockDim.x);
 }
 
 __device__ __forceinline__ void cell_of(const ColView& C, int v, long long* c) {
@@ -123,9 +133,7 @@ __device__ __forceinline__ void cell_of(const ColView& C, int v, long long* c) {
   c[2] = (long long)floor(cpos(C, v, 2) / C.cell);
 }
 
-__global__ void c_insert(ColView C) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
+__device__ void c_insert_one(const ColView& C, int v) {
   if (v >= C.nv || !is_surface(C, v)) return;
   C.lastWatch[v] = (float)cpos(C, v, 0);
   C.lastWatch[C.nv + v] = (float)cpos(C, v, 1);
@@ -143,6 +151,9 @@ __global__ void c_insert(ColView C) {
     h = (h + 1) & C.hcap_mask;
   }
   atomicOr(&C.cc->status, VXG_COL_ST_HASH_FULL);
+}
+__global__ void c_insert(ColView C) {
+  if (c_rebuilding(C)) c_insert_one(C, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 __device__ __forceinline__ int find_cell(const ColView& C, unsigned long long k) {
@@ -188,19 +199,20 @@ __device__ __forceinline__ void for_partners(const ColView& C, int v, F&& f) {
       }
 }
 
-__global__ void c_count(ColView C) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
+__device__ void c_count_one(const ColView& C, int v) {
   if (v >= C.nv) return;
   int all = 0, gt = 0;
   if (is_surface(C, v)) for_partners(C, v, [&](int u) { all++; gt += u > v; });
   C.cntAll[v] = all;
   C.cntGt[v] = gt;
 }
+__global__ void c_count(ColView C) {
+  if (c_rebuilding(C)) c_count_one(C, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-// exclusive scans of cntGt -> pairOff and cntAll -> watchOff (one block; rebuilds are rare)
-__global__ void c_scan(ColView C) {
-  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged) return;
+// exclusive scans of cntGt -> pairOff and cntAll -> watchOff by one block of up to 1024 threads
+// (rebuilds are rare)
+__device__ void c_scan_block(const ColView& C) {
   __shared__ int sg[1024], sa[1024];
   int t = threadIdx.x, T = blockDim.x;
   int chunk = (C.nv + T - 1) / T;
@@ -233,10 +245,11 @@ __global__ void c_scan(ColView C) {
     if (sa[t] > C.wcap) atomicOr(&C.cc->status, VXG_COL_ST_WATCH_OVERFLOW);
   }
 }
+__global__ void c_scan(ColView C) {
+  if (c_rebuilding(C)) c_scan_block(C);
+}
 
-__global__ void c_fill(ColView C) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged || C.cc->status) return;
+__device__ void c_fill_one(const ColView& C, int v) {
   if (v >= C.nv || !is_surface(C, v)) return;
   int buf[kMaxPartners];
   int n = 0;
@@ -269,10 +282,11 @@ __global__ void c_fill(ColView C) {
     }
   }
 }
+__global__ void c_fill(ColView C) {
+  if (c_rebuilding(C) && !C.cc->status) c_fill_one(C, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-__global__ void c_watch(ColView C) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!C.cc->stale || C.ctl->halt || C.ctl->diverged || C.cc->status) return;
+__device__ void c_watch_one(const ColView& C, int v) {
   if (v >= C.nv) return;
   int wo = C.watchOff[v], n = C.cntAll[v];
   int nLess = n - C.cntGt[v];
@@ -294,6 +308,31 @@ __global__ void c_watch(ColView C) {
     }
     C.watchItem[wo + k] = item;
   }
+}
+__global__ void c_watch(ColView C) {
+  if (c_rebuilding(C) && !C.cc->status) c_watch_one(C, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// The whole rebuild in one cooperative launch: the phases above, separated by grid-wide barriers
+// (a cooperative launch keeps every block resident, so the barriers end).  When the list is not
+// stale every block returns at once, so a step pays one launch instead of six.
+__global__ void __launch_bounds__(256) c_rebuild(ColView C) {
+  if (!c_rebuilding(C)) return;  // uniform: no block reaches a barrier unless all do
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  c_clear_range(C, first, stride);
+  grid.sync();
+  for (int v = first; v < C.nv; v += stride) c_insert_one(C, v);
+  grid.sync();
+  for (int v = first; v < C.nv; v += stride) c_count_one(C, v);
+  grid.sync();
+  if (blockIdx.x == 0) c_scan_block(C);
+  grid.sync();
+  if (C.cc->status) return;  // written before the last barrier: the same for every block
+  for (int v = first; v < C.nv; v += stride) c_fill_one(C, v);
+  grid.sync();
+  if (C.cc->status) return;
+  for (int v = first; v < C.nv; v += stride) c_watch_one(C, v);
 }
 
 // CVX_Voxel::baseSizeAverage for the envelope  VX_Voxel.h:90
@@ -425,6 +464,7 @@ struct Collide {
     C.watchOff = C.watchItem = nullptr;
     C.pairForce = nullptr;
     nv = n;
+    coop_blocks = -1;
     if (!cc) {
       if (cudaMalloc(&cc, sizeof(ColCtl)) != cudaSuccess) return VXG_E_CUDA;
     }
@@ -528,7 +568,31 @@ struct Collide {
     C.s64 = g.voxSize;
     C.s32 = (float)g.voxSize;
   }
-  void enqueue_rebuild(cudaStream_t s) {
+  // the cooperative rebuild: blocks resident on the whole GPU (0: launch the six kernels instead)
+  int coop_blocks = -1;
+  int coop_grid() {
+    if (coop_blocks < 0) {
+      int dev = 0, n_sm = 1, coop = 0, per_sm = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+      if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c_rebuild, 256, 0) == cudaSuccess && per_sm > 0)
+        coop_blocks = std::min(n_sm * per_sm, std::max(1, (nv + 255) / 256));
+      else
+        coop_blocks = 0;
+      cudaGetLastError();
+    }
+    return coop_blocks;
+  }
+  // returns the number of kernels launched
+  int enqueue_rebuild(cudaStream_t s) {
+    const int gb = coop_grid();
+    if (gb > 0) {
+      void* args[] = {&C};
+      if (cudaLaunchCooperativeKernel((const void*)c_rebuild, dim3(gb), dim3(256), args, 0, s) == cudaSuccess) return 1;
+      cudaGetLastError();
+      coop_blocks = 0;  // not available here: the separate kernels from now on
+    }
     int gv = std::max(1, (nv + 255) / 256);
     c_clear<<<256, 256, 0, s>>>(C);
     c_insert<<<gv, 256, 0, s>>>(C);
@@ -536,18 +600,19 @@ struct Collide {
     c_scan<<<1, 1024, 0, s>>>(C);
     c_fill<<<std::max(1, (nv + 127) / 128), 128, 0, s>>>(C);  // 128 threads: 512 B of partners each
     c_watch<<<gv, 256, 0, s>>>(C);
+    return 6;
   }
-  // Launches the stage on stream s; returns the number of kernels launched.  The rebuild kernels
-  // exit at once unless c_check found the pair list stale.  (A conditional graph node around them
-  // measured slower than these early exits on GB300.)
+  // Launches the stage on stream s; returns the number of kernels launched.  The rebuild exits at
+  // once unless c_check found the pair list stale.  (A conditional graph node around separate
+  // rebuild kernels measured slower than their early exits on GB300.)
   int enqueue(const vxg_globals& g, cudaStream_t s) {
     if (!buf || !C.nbOff) return 0;
     set_globals(g);
     int gv = std::max(1, (nv + 255) / 256);
     c_check<<<gv, 256, 0, s>>>(C);
-    enqueue_rebuild(s);
+    int n = enqueue_rebuild(s);
     c_contact<<<grid_pairs, 256, 0, s>>>(C);
-    return 8;
+    return 2 + n;
   }
   int get_pairs(int* out, int cap, int* n, cudaStream_t s) {
     *n = 0;
