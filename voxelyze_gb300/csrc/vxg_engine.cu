@@ -1320,6 +1320,15 @@ static int lp_resident(vxg_engine* e, bool pois) {
   return std::max(1, e->n_sm) * bps;
 }
 
+// a timing event between two passes; inside a stream capture it becomes an event-record node of
+// the graph, so the GPU records it between the kernels with no host in between
+static void pass_event(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &st);
+  if (st == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal);
+  else cudaEventRecord(ev, s);
+}
+
 static bool fused_poisson(const vxg_engine* e) {
   return e->precision == VXG_FP32C && e->tab_poisson && e->poisson_fuse;
 }
@@ -1339,7 +1348,7 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   bool rec = dt < 0;
   const int bl = e->blk_link, bv = e->blk_voxel;
   const int gl = grid_of(e->nl, bl), gv = grid_of(e->nv, bv);
-  if (ev) cudaEventRecord(ev[0], e->stream);
+  if (ev) pass_event(ev[0], e->stream);
   // kernels this step launches (or, under capture, records)
   (void)first;
   long long nk = 1 + (e->nl ? 1 : 0) + (e->act_mode && e->nv ? 1 + (e->nl ? 1 : 0) : 0) +
@@ -1372,9 +1381,9 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
         else k_link32<false, true, false><<<gl, bl, 0, e->stream>>>(e->V, parity);
       }
     }
-    if (ev) cudaEventRecord(ev[1], e->stream);
+    if (ev) pass_event(ev[1], e->stream);
     if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream);
-    if (ev) cudaEventRecord(ev[2], e->stream);
+    if (ev) pass_event(ev[2], e->stream);
     e->n_launch += nk;
     if (fused_poisson(e)) {
       if (rec) k_voxel32<true, true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
@@ -1383,20 +1392,20 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
       if (rec) k_voxel32<true, false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
       else k_voxel32<false, false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
     }
-    if (ev) cudaEventRecord(ev[3], e->stream);
+    if (ev) pass_event(ev[3], e->stream);
     return;
   }
   if (e->nl) {
     if (rec) k_link<true, true><<<gl, bl, 0, e->stream>>>(S, parity);
     else k_link<false, true><<<gl, bl, 0, e->stream>>>(S, parity);
   }
-  if (ev) cudaEventRecord(ev[1], e->stream);
+  if (ev) pass_event(ev[1], e->stream);
   if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream);
-  if (ev) cudaEventRecord(ev[2], e->stream);
+  if (ev) pass_event(ev[2], e->stream);
   e->n_launch += nk;
   if (rec) k_voxel<true><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
   else k_voxel<false><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
-  if (ev) cudaEventRecord(ev[3], e->stream);
+  if (ev) pass_event(ev[3], e->stream);
 }
 
 static int capture(vxg_engine* e, int n, float dt, cudaGraphExec_t* out) {
@@ -1478,7 +1487,18 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
       VXG_CK(cudaEventCreate(&x));
       e->tev.push_back(x);
     }
+    // the steps with their per-pass events, captured and replayed once so that the events time
+    // the kernels, not the host's launch gaps
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    VXG_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == 0, &e->tev[(size_t)4 * s]);
+    cudaError_t c = cudaStreamEndCapture(e->stream, &g);
+    if (c == cudaSuccess) c = cudaGraphInstantiate(&x, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (c == cudaSuccess) c = cudaGraphLaunch(x, e->stream);
+    if (x) cudaGraphExecDestroy(x);
+    if (c != cudaSuccess) return fail(e, VXG_E_CUDA, "timed batch", c);
     e->tev_used = nsteps;
   } else {
     for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == 0);
