@@ -236,10 +236,18 @@ VX_HD LinkIn link_gather(const View& S, int l) {
   in.lmat = B.lmat[l];
   in.rd = S.restDelta[l];
   in.oldPos2 = ld3(S.pos2, nl, l);
-  in.oldA1 = ld3(S.a1v, nl, l);
+  // a small-angle link's angle1 is the identity, so its stored rotation vector is zero
+  // (CVX_Link::orientLink, src/VX_Link.cpp:101-111; a new link starts small-angle with zeros, :63-68)
+  in.oldA1 = (in.lf & VXG_LF_SMALL_ANGLE) ? F3(0, 0, 0) : ld3(S.a1v, nl, l);
   in.oldA2 = ld3(S.a2v, nl, l);
-  in.tArea = B.tArea[l];
-  in.tSS = B.tSS[l];
+  // the stored transverse terms are used only where the link material has nu == 0; otherwise
+  // updateForces recomputes both before any use (src/VX_Link.cpp:160)
+  if (!POIS || B.lm[in.lmat].nu == 0.0f) {
+    in.tArea = B.tArea[l];
+    in.tSS = B.tSS[l];
+  } else {
+    in.tArea = in.tSS = 0.0f;
+  }
   in.maxStrain = B.maxStrain[l];
   in.strainOffset = B.strainOffset[l];
   int vn = B.lvox[l], vp = B.lvox[nl + l];
@@ -310,7 +318,7 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
   f3 a1v = to_rotation_vector(angle1);
   f3 a2v = to_rotation_vector(angle2);
   st3(S.pos2, nl, l, pos2);
-  st3(S.a1v, nl, l, a1v);
+  if (!(smallAngle && (lf & VXG_LF_SMALL_ANGLE))) st3(S.a1v, nl, l, a1v);  // else zeros, already stored
   st3(S.a2v, nl, l, a2v);
   f3 dPos2 = F3(0.5f * (pos2.x - oldPos2.x), 0.5f * (pos2.y - oldPos2.y), 0.5f * (pos2.z - oldPos2.z));
   f3 dA1 = F3(0.5f * (a1v.x - oldA1.x), 0.5f * (a1v.y - oldA1.y), 0.5f * (a1v.z - oldA1.z));

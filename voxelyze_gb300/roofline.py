@@ -36,10 +36,12 @@ def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
 
 
 # FP32C layout (voxelyze_gb300/csrc/vx_phys32.cuh):
-#   link pass, per link : endpoint ids 8, flags 4 read, material id 4, previous pos2/angle1v/angle2v
-#                         36 read + 36 written, rest offset 4, transverse area/strain sum 8 read +
-#                         8 written, maxStrain/strainOffset 8 read, strain and stress 8 written,
-#                         forces and moments 48 written                                   = 176 B
+#   link pass, per link : endpoint ids 8, flags 4 read, material id 4, previous pos2/angle2v 24 read
+#                         + 24 written, rest offset 4, transverse area/strain sum 8 (written where
+#                         the link material has nu != 0, read where nu == 0), maxStrain/strainOffset
+#                         8 read, strain and stress 8 written, forces and moments 48 written = 144 B
+#                         + previous angle1v 12 read + 12 written per large-angle link (a small-
+#                         angle link's is zero: neither read nor rewritten while it stays small)
 #                         (flags, maxStrain and strainOffset are written only when they change,
 #                         which is rare, so those writes are not counted)
 #             per voxel : displacement 12, orientation 16, material id 4                  =  32 B
@@ -50,7 +52,8 @@ def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
 #             per link  : the force and moment each end gathers, 2 x 24                   =  48 B
 #   Poisson cache (nu != 0), filled by the voxel pass for the next step: cached strain 12 B written
 #                         per voxel, strain and strain ratio 8 B per link gathered
-FP32C_LINK_PER_LINK = 176
+FP32C_LINK_PER_LINK = 144
+FP32C_LINK_PER_LARGE_ANGLE_LINK = 24
 FP32C_LINK_PER_VOXEL = 32
 FP32C_LINK_PER_VOXEL_POISSON = 12
 FP32C_VOXEL_PER_VOXEL = 208
@@ -59,8 +62,9 @@ FP32C_VOXEL_PER_VOXEL_POISSON = 12
 FP32C_VOXEL_PER_LINK_POISSON = 8
 
 
-def fp32c_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
-    link = FP32C_LINK_PER_LINK * n_links + FP32C_LINK_PER_VOXEL * n_voxels
+def fp32c_bytes(n_voxels: int, n_links: int, poisson: bool, large_angle_links: int = 0) -> dict:
+    link = (FP32C_LINK_PER_LINK * n_links + FP32C_LINK_PER_LARGE_ANGLE_LINK * large_angle_links
+            + FP32C_LINK_PER_VOXEL * n_voxels)
     voxel = FP32C_VOXEL_PER_VOXEL * n_voxels + FP32C_VOXEL_PER_LINK * n_links
     if poisson:
         link += FP32C_LINK_PER_VOXEL_POISSON * n_voxels
