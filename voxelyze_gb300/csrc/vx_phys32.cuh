@@ -570,7 +570,7 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
       nf = (nf & ~(uint32_t)VXG_VF_PSTRAIN_INVALID) | VXG_VF_PSTRAIN_EAGER;
     }
   }
-  B.vflags[v] = nf;
+  if (nf != flags) B.vflags[v] = nf;  // the flags change rarely (friction latch, Poisson cache state)
 }
 
 }  // namespace vx32

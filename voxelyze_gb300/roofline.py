@@ -47,8 +47,8 @@ def fp64_bytes(n_voxels: int, n_links: int, poisson: bool) -> dict:
 #             per voxel : displacement 12, orientation 16, material id 4                  =  32 B
 #                         (+ the cached Poisson strain 12 when nu != 0)
 #   voxel pass, per voxel: displacement and orientation with their compensations, momenta 80 read
-#                         + 80 written, flags 4+4, material id 4, external id 4, 6 link ids 24,
-#                         lattice z 4, temperature 4                                     = 208 B
+#                         + 80 written, flags 4 read (written only when they change), material id
+#                         4, external id 4, 6 link ids 24, lattice z 4, temperature 4     = 204 B
 #             per link  : the force and moment each end gathers, 2 x 24                   =  48 B
 #   Poisson cache (nu != 0), filled by the voxel pass for the next step: cached strain 12 B written
 #                         per voxel, strain and strain ratio 8 B per link gathered
@@ -56,7 +56,7 @@ FP32C_LINK_PER_LINK = 144
 FP32C_LINK_PER_LARGE_ANGLE_LINK = 24
 FP32C_LINK_PER_VOXEL = 32
 FP32C_LINK_PER_VOXEL_POISSON = 12
-FP32C_VOXEL_PER_VOXEL = 208
+FP32C_VOXEL_PER_VOXEL = 204
 FP32C_VOXEL_PER_LINK = 48
 FP32C_VOXEL_PER_VOXEL_POISSON = 12
 FP32C_VOXEL_PER_LINK_POISSON = 8
