@@ -122,20 +122,24 @@ def _fp32c(product_lib, scene, blocks_per_sm):
     return s
 
 
-@pytest.mark.parametrize("scene", ["lattice_poisson", "cantilever", "population_actuated", "graded"])
+@pytest.mark.parametrize("scene", ["lattice_poisson", "cantilever", "population_actuated", "graded", "floppy"])
 @pytest.mark.parametrize("blocks_per_sm", [-1, 1])
 def test_pipelined_link_pass_is_bit_identical(product_lib, scene, blocks_per_sm):
     """The pipelined FP32C link pass (cp.async staging, resident grid) against the one-thread-per-
     link pass: every state array identical bit for bit after each batch.  One block per SM makes
     every block walk many tiles (both halves of the double buffer); the scenes cover Poisson's
     ratio != 0 with bilinear materials, a fixed cantilever, in-step CTE actuation with floor and
-    friction, and one material per voxel."""
+    friction, and one material per voxel.  The floppy beam (20 voxels in a row, E = 10 kPa) moves
+    links into and out of the large-angle branch all through the run: the pipelined pass always
+    reads each link's stored angle1v, the other pass takes it as zero while a link stays small-
+    angle, so identical states also check that the stored angle1v of a small-angle link is zero."""
     from conftest import state_diff
 
     sc = {"lattice_poisson": lambda: S.lattice(40, 36, 20),
           "cantilever": lambda: S.cantilever(40, 8, 8),
           "population_actuated": lambda: S.population(24, 4, 12),
-          "graded": lambda: S.graded_population(6, 10)}[scene]()
+          "graded": lambda: S.graded_population(6, 10),
+          "floppy": lambda: S.cantilever(20, 1, 1, E=1e4, tip_force=-0.02)}[scene]()
     a = _fp32c(product_lib, sc, 0)
     b = _fp32c(product_lib, sc, blocks_per_sm)
     dt = a.recommended_time_step()
@@ -143,9 +147,14 @@ def test_pipelined_link_pass_is_bit_identical(product_lib, scene, blocks_per_sm)
     if scene in ("population_actuated", "graded"):
         for s in (a, b):
             F.Engine(s).set_actuation(F.ACT_UNIFORM, 0.1, 2.0)
-    for _ in range(3):
-        assert a.do_time_steps(70, dt) == b.do_time_steps(70, dt) == 70
+    n, batches = (250, 8) if scene == "floppy" else (70, 3)
+    large = 0
+    for _ in range(batches):
+        assert a.do_time_steps(n, dt) == b.do_time_steps(n, dt) == n
         assert state_diff(a, b) == []
+        large += int((a.link_state()["smallAngle"] == 0).sum())
+    if scene == "floppy":
+        assert large > 0
 
 
 def _dynamic_state(s):
