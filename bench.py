@@ -447,7 +447,12 @@ def run_adjoint(args, world, rank, local):
     bodies = rng.choice(len(off) - 1, size=64, replace=False)
     pick = [(int(b), int(rng.integers(off[b], off[b + 1])), "E" if i % 2 == 0 else "phase")
             for i, b in enumerate(bodies)]
-    rows, _, t_adj, dt = G.check(lib, sc, nsteps, K, pick, 1e-3, 1e-2)
+    ad, obj, t_adj, dt, dec = G.adjoint(lib, sc, nsteps, K, pick)
+    rows = G.differences(lib, sc, pick, nsteps, dt, ad, 1e-3, 1e-2)
+    # the same parameters with the plain run's contact and friction decisions replayed, wider steps,
+    # Richardson-extrapolated
+    frozen = G.differences(lib, sc, pick, nsteps, dt, ad, 1.6e-2, 0.16, decisions=dec)
+    fe = np.array([r["richardson_error"] for r in frozen])
     sim, _ = G.build(lib, sc, sc.phase, 0.1, 2.0)
     sim.recommended_time_step()
     t0 = time.perf_counter()
@@ -476,7 +481,15 @@ def run_adjoint(args, world, rank, local):
                                           "distance_median": float(np.median(d)),
                                           "distance_p90": float(np.percentile(d, 90)),
                                           "distance_max": float(d.max()),
-                                          "within_1e-4": float(np.mean(d <= 1e-4))}},
+                                          "within_1e-4": float(np.mean(d <= 1e-4))},
+                       "gradient_check_frozen_decisions": {
+                           "parameters": len(frozen),
+                           "fd_steps": "1.6e-2 relative (E), 0.16 rad (phase), and a quarter of each, with the "
+                                       "plain run's floor-contact and static-friction decisions replayed; "
+                                       "Richardson-extrapolated",
+                           "error_median": float(np.median(fe)), "error_p90": float(np.percentile(fe, 90)),
+                           "error_max": float(fe.max()), "within_1e-4": float(np.mean(fe <= 1e-4)),
+                           "within_1e-3": float(np.mean(fe <= 1e-3))}},
             "cpu_baseline": cpu, "timing": "host wall clock around vxg_adjoint_com_x (synchronous)"}
     print(json.dumps(line))
 

@@ -98,6 +98,9 @@ int vx_autotune(void* s, int trial_steps, float dt, int* out3);            /* vx
 int vx_set_link_pipeline(void* s, int blocks_per_sm);                      /* vxg_set_link_pipeline */
 int vx_get_link_pipeline(void* s, int* blocks_per_sm);                     /* vxg_get_link_pipeline */
 int vx_set_poisson_fusion(void* s, int on);                                /* vxg_set_poisson_fusion */
+int vx_set_decisions(void* s, int mode, long long steps);                  /* vxg_set_decisions */
+int vx_get_decisions(void* s, unsigned char* out, long long steps);        /* vxg_get_decisions */
+int vx_put_decisions(void* s, const unsigned char* in, long long steps);   /* vxg_put_decisions */
 
 #ifdef __cplusplus
 }

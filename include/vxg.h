@@ -212,6 +212,17 @@ int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_
  * Both give identical results. */
 int vxg_set_link_pipeline(vxg_engine* e, int blocks_per_sm);
 int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm);
+/* Branch decisions of the FP64 voxel pass (no counterpart in the reference), for finite differences
+ * that follow one run's branches: mode 1 records, for each of the next `steps` steps, every voxel's
+ * floor-contact and static-friction decisions (CVX_Voxel::floorForce and the static-friction latch
+ * of CVX_Voxel::timeStep, src/VX_Voxel.cpp:188-199, 274-298; one byte per voxel per step); mode 2
+ * replays them (the run takes the recorded branches instead of comparing); 0 stops.  Setting a mode
+ * restarts at the first row; a batch longer than the rows left fails with VXG_E_SIZE; steps run
+ * one launch at a time meanwhile.  vxg_get_decisions / vxg_put_decisions copy the first `steps` rows
+ * (steps * n_voxels bytes) out of or into the engine. */
+int vxg_set_decisions(vxg_engine* e, int mode, long long steps);
+int vxg_get_decisions(vxg_engine* e, unsigned char* host, long long steps);
+int vxg_put_decisions(vxg_engine* e, const unsigned char* host, long long steps);
 /* FP32C with Poisson's ratio != 0: on (the default), the voxel pass fills each voxel's Poisson-
  * strain cache for the next step's link pass from that step's link strains (CVX_Voxel::strain,
  * src/VX_Voxel.cpp:300-343, which the reference evaluates lazily in the next link pass); off, a

@@ -80,6 +80,44 @@ def test_adjoint_config5_horizon(product_lib):
     assert np.percentile(d, 90) <= 1e-2
 
 
+def test_adjoint_against_frozen_decision_differences(product_lib):
+    """12 bodies of 8^3 cells, 1,000 steps.  The perturbed runs replay the unperturbed run's
+    floor-contact and static-friction decisions (vxg_set_decisions), so the differences measure the
+    derivative along the branches the adjoint follows, and the O(h^2) truncation of the two central
+    differences (h = 1.6e-2 relative for E and density, 0.16 rad for phases, and a quarter of each)
+    is removed by Richardson extrapolation.  Every parameter then agrees with the adjoint; the
+    remaining error is the differences' own noise from the float roundings of the reference's
+    arithmetic (replaying a run's own decisions reproduces it bit for bit, checked first)."""
+    sc = S.graded_population(12, 8, 0.7, seed=12)
+    off = G.body_offsets(sc)
+    rng = np.random.default_rng(1)
+    kinds = ["E", "rho", "phase"]
+    pick = [(b, int(rng.integers(off[b], off[b + 1])), kinds[b % 3]) for b in range(len(off) - 1)]
+    rows, _, _, _ = G.check(product_lib, sc, 1000, 100, pick, 1.6e-2, 0.16, AMP, FREQ, frozen=True)
+    err = np.array([r["richardson_error"] for r in rows])
+    for (b, v, kind), r in zip(pick, rows):
+        print("body %3d voxel %5d d/d%-5s adjoint % .6e extrapolated % .6e error %.2e"
+              % (b, v, kind, r["adjoint"], r["richardson"], r["richardson_error"]))
+    print(f"frozen decisions: error median {np.median(err):.2e}, max {err.max():.2e}")
+    assert np.median(err) <= 1e-4
+    assert err.max() <= 5e-4
+
+
+def test_decision_replay_follows_the_recorded_branches(product_lib):
+    """Replaying a run's own decisions reproduces it bit for bit; a perturbed scene, left to decide
+    for itself, takes other branches (which replay holds to the recorded ones)."""
+    sc = S.graded_population(4, 6, 0.7, seed=5)
+    off = G.body_offsets(sc)
+    g, _ = G.build(product_lib, sc, sc.phase, AMP, FREQ)
+    dt = g.recommended_time_step()
+    base, dec = G.body_com_x(product_lib, sc, sc.phase, 400, dt, off, AMP, FREQ, record=True)
+    assert dec.shape == (400, sc.n_voxels) and (dec & 1).any() and (dec & 2).any()
+    assert np.array_equal(G.body_com_x(product_lib, sc, sc.phase, 400, dt, off, AMP, FREQ, decisions=dec), base)
+    ph = (sc.phase + np.float32(0.5)).astype(np.float32)
+    _, own = G.body_com_x(product_lib, sc, ph, 400, dt, off, AMP, FREQ, record=True)
+    assert not np.array_equal(own, dec)
+
+
 def test_adjoint_rejects_out_of_scope(product_lib):
     sc = S.graded_population(2, 4, 0.7, seed=3)
     sc.materials[0].nu = 0.3

@@ -1529,6 +1529,19 @@ int vx_set_poisson_fusion(void* s, int on) {
   if (!vx.upload()) return -1;
   return vxg_set_poisson_fusion(vx.impl()->eng, on) ? -1 : 0;
 }
+int vx_set_decisions(void* s, int mode, long long steps) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_set_decisions(vx.impl()->eng, mode, steps) ? -1 : 0;
+}
+int vx_get_decisions(void* s, unsigned char* out, long long steps) {
+  vxg_engine* e = H(s)->vx.impl()->eng;
+  return e && vxg_get_decisions(e, out, steps) == 0 ? 0 : -1;
+}
+int vx_put_decisions(void* s, const unsigned char* in, long long steps) {
+  vxg_engine* e = H(s)->vx.impl()->eng;
+  return e && vxg_put_decisions(e, in, steps) == 0 ? 0 : -1;
+}
 int vx_get_link_pipeline(void* s, int* blocks_per_sm) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.upload()) return -1;

@@ -468,7 +468,13 @@ VX_HDN void link_update(const View& S, int l) {
 }
 
 // CVX_Voxel::timeStep + force + moment + floorForce  VX_Voxel.cpp:162-298
-VX_HDN void voxel_update(const View& S, int v, float dt) {
+// DEC 0 takes the floor-contact and static-friction decisions as the reference does.  DEC 1 also
+// records them in *dec: bit 0 the voxel touches the floor (penetration >= 0), bit 1 static friction
+// holds at the end of the step.  DEC 2 replays them from *dec instead of comparing, so a perturbed
+// run follows the recorded run's branches (finite differences of the branch an adjoint
+// differentiates); the forces are still evaluated from the perturbed state.
+template <int DEC = 0>
+VX_HDN void voxel_update(const View& S, int v, float dt, uint8_t* dec = nullptr) {
   const int nv = S.nv;
   S.prevDt[v] = dt;
   if (dt == 0.0f) return;
@@ -525,14 +531,14 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   double bsa = base_size_avg(S, v);
   if (floorOn) {
     float pen = (float)(bsa / 2 - m.nomSize / 2 - pos.z);
-    if (pen >= 0) {
+    if (DEC == 2 ? (*dec & 1) != 0 : pen >= 0) {
       d3 vel = D3(m.massInv * lin.x, m.massInv * lin.y, m.massInv * lin.z);
       float normal = m.penetrationStiffness * pen;
       F.z += normal - (m.zetaCollision * m.c2xSqMxExS) * vel.z;
       if (staticF) {
         float surf = (float)(F.x * F.x + F.y * F.y);
         float fr = (m.muStatic * normal) * (m.muStatic * normal);
-        if (surf > fr) staticF = false;
+        if (DEC != 2 && surf > fr) staticF = false;
       } else {
         float k = m.muKinetic * normal;
         d3 h = D3(vel.x, vel.y, 0);
@@ -551,10 +557,12 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   lin.x += dt * F.x; lin.y += dt * F.y; lin.z += dt * F.z;
   float dtm = dt * m.massInv;
   d3 tr = D3(dtm * lin.x, dtm * lin.y, dtm * lin.z);
-  if (floorOn && (float)(bsa / 2 - m.nomSize / 2 - pos.z) >= 0) {
+  const bool contact = floorOn && (DEC == 2 ? (*dec & 1) != 0 : (float)(bsa / 2 - m.nomSize / 2 - pos.z) >= 0);
+  if (contact) {
     double work = fric.x * tr.x + fric.y * tr.y;
     double hKe = 0.5 * m.massInv * (lin.x * lin.x + lin.y * lin.y);
-    if (hKe + work <= 0) staticF = true;
+    if (DEC == 2) staticF = (*dec & 2) != 0;
+    else if (hKe + work <= 0) staticF = true;
     if (staticF) {
       lin.x = lin.y = 0;
       tr.x = tr.y = 0;
@@ -562,6 +570,7 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   } else {
     staticF = false;
   }
+  if (DEC == 1) *dec = (uint8_t)((contact ? 1 : 0) | (staticF ? 2 : 0));
   pos.x += tr.x; pos.y += tr.y; pos.z += tr.z;
 
   // moment()  VX_Voxel.cpp:258-271

@@ -93,8 +93,9 @@ __device__ __forceinline__ float step_dt(const View& S, bool recommend, float dt
   return 1.0f / (6.283185f * sqrtf(mx));
 }
 
-template <bool RECOMMEND>
-__global__ void __launch_bounds__(512) k_voxel(View S, float dt_fixed, int parity, float fallback) {
+template <bool RECOMMEND, int DEC = 0>
+__global__ void __launch_bounds__(512) k_voxel(View S, float dt_fixed, int parity, float fallback,
+                                               uint8_t* dec = nullptr) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (S.ctl->halt) return;
   if (S.ctl->diverged) {
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(512) k_voxel(View S, float dt_fixed, int parit
     if (RECOMMEND) S.ctl->maxf[parity ^ 1] = 0u;  // next step's slot; nobody reads it in this pass
   }
   if (v >= S.nv) return;
-  vx64::voxel_update(S, v, dt);
+  vx64::voxel_update<DEC>(S, v, dt, DEC ? dec + v : nullptr);
 }
 
 // setAmbientTemperature(t, true): every voxel's temperature, then every link's rest length
@@ -773,6 +774,11 @@ struct vxg_engine {
   int* h_ctl = nullptr;      // pinned copy of the batch's control words
   // kernels launched by the time step (a graph replay counts the kernels it holds)
   long long n_launch = 0, graph_kernels = 0, cgraph_kernels = 0;
+  // FP64 branch decisions (vxg_set_decisions): 0 off, 1 record, 2 replay; one byte per voxel per
+  // step for dec_cap steps; dec_step is the next step's row
+  int dec_mode = 0;
+  uint8_t* d_dec = nullptr;
+  long long dec_cap = 0, dec_step = 0;
   // per-step actuation (vxg_set_actuation)
   int act_mode = 0;
   double act_amp = 0, act_freq = 0;
@@ -1029,6 +1035,7 @@ int vxg_destroy(vxg_engine* e) {
   if (e->d_powtab) cudaFree(e->d_powtab);
   if (e->d_sp_idx) cudaFree(e->d_sp_idx);
   if (e->d_sp_t) cudaFree(e->d_sp_t);
+  if (e->d_dec) cudaFree(e->d_dec);
   for (void* p : {(void*)e->d_mesh_vv, (void*)e->d_mesh_quads, (void*)e->d_mesh_vert, (void*)e->d_mesh_norm})
     if (p) cudaFree(p);
   if (e->d_partials) cudaFree(e->d_partials);
@@ -1403,8 +1410,20 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream);
   if (ev) pass_event(ev[2], e->stream);
   e->n_launch += nk;
-  if (rec) k_voxel<true><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
-  else k_voxel<false><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+  if (e->dec_mode) {  // one row of branch decisions per step (vxg_step checked the capacity)
+    uint8_t* row = e->d_dec + (size_t)e->dec_step++ * (size_t)e->nv;
+    if (e->dec_mode == 1) {
+      if (rec) k_voxel<true, 1><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2, row);
+      else k_voxel<false, 1><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2, row);
+    } else {
+      if (rec) k_voxel<true, 2><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2, row);
+      else k_voxel<false, 2><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2, row);
+    }
+  } else if (rec) {
+    k_voxel<true><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+  } else {
+    k_voxel<false><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+  }
   if (ev) pass_event(ev[3], e->stream);
 }
 
@@ -1444,7 +1463,10 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
                 "control block layout");
   VXG_CK(cudaMemsetAsync(e->ctl, 0, offsetof(Ctl, time), e->stream));
   poisson_refill(e);
-  bool use_graph = e->timing != 1 && nsteps > 1;
+  if (e->dec_mode && e->dec_step + nsteps > e->dec_cap)
+    return fail(e, VXG_E_SIZE, "vxg_step: more steps than the branch-decision rows set aside");
+  // branch decisions take a row pointer per step: launched step by step, never captured
+  bool use_graph = e->timing != 1 && nsteps > 1 && !e->dec_mode;
   if (e->timing == 2) {
     for (int k = 0; k < 2; ++k)
       if (!e->bev[k]) VXG_CK(cudaEventCreate(&e->bev[k]));
@@ -1480,7 +1502,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
       VXG_CK(cudaGraphLaunch(e->graph, e->stream));
       e->n_launch += e->graph_kernels;
     }
-  } else if (e->timing == 1) {
+  } else if (e->timing == 1 && !e->dec_mode) {
     size_t need = (size_t)4 * nsteps;
     while (e->tev.size() < need) {
       cudaEvent_t x;
@@ -1787,6 +1809,38 @@ int vxg_set_poisson_fusion(vxg_engine* e, int on) {
     e->poisson_redo = true;  // caches filled ahead of time are refilled at the lazy point
     e->graph_valid = false;
   }
+  return VXG_OK;
+}
+int vxg_set_decisions(vxg_engine* e, int mode, long long steps) {
+  if (!e || mode < 0 || mode > 2 || steps < 0) return VXG_E_ARG;
+  if (mode && e->precision != VXG_FP64) return fail(e, VXG_E_STATE, "vxg_set_decisions: the FP64 path records decisions");
+  VXG_CK(cudaSetDevice(e->device));
+  if (mode && steps > e->dec_cap) {
+    if (e->d_dec) cudaFree(e->d_dec);
+    e->d_dec = nullptr;
+    e->dec_cap = 0;
+    VXG_CK(cudaMalloc(&e->d_dec, std::max<size_t>(1, (size_t)steps * (size_t)e->nv)));
+    e->dec_cap = steps;
+  }
+  e->dec_mode = mode;
+  e->dec_step = 0;
+  e->graph_valid = false;
+  return VXG_OK;
+}
+int vxg_get_decisions(vxg_engine* e, unsigned char* host, long long steps) {
+  if (!e || !host || steps < 0 || steps > e->dec_cap) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  if (steps && e->nv)
+    VXG_CK(cudaMemcpyAsync(host, e->d_dec, (size_t)steps * (size_t)e->nv, cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  return VXG_OK;
+}
+int vxg_put_decisions(vxg_engine* e, const unsigned char* host, long long steps) {
+  if (!e || !host || steps < 0 || steps > e->dec_cap) return VXG_E_ARG;
+  VXG_CK(cudaSetDevice(e->device));
+  if (steps && e->nv)
+    VXG_CK(cudaMemcpyAsync(e->d_dec, host, (size_t)steps * (size_t)e->nv, cudaMemcpyHostToDevice, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
   return VXG_OK;
 }
 int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm) {

@@ -324,6 +324,9 @@ _EXT_SIGS = {
     "autotune": (_i, [_p, _i, _f, _ip]),
     "set_link_pipeline": (_i, [_p, _i]),
     "get_link_pipeline": (_i, [_p, _ip]),
+    "set_decisions": (_i, [_p, _i, C.c_longlong]),
+    "get_decisions": (_i, [_p, C.POINTER(C.c_ubyte), C.c_longlong]),
+    "put_decisions": (_i, [_p, C.POINTER(C.c_ubyte), C.c_longlong]),
     "set_poisson_fusion": (_i, [_p, _i]),
     "adjoint_com_x": (_i, [_p, _i, _f, _i, _ip, _i, _dp, _dp, _dp, _dp]),
 }
@@ -381,6 +384,20 @@ class Engine:
         """FP32C, nu != 0: fill the Poisson-strain cache in the voxel pass (default) or in a
         pre-pass before every link pass; the trajectories are identical."""
         self._ck(self.f["set_poisson_fusion"](self.sim.h, 1 if on else 0))
+
+    def set_decisions(self, mode: int, steps: int = 0):
+        """FP64: 1 records the floor-contact and static-friction decisions of the next `steps`
+        steps (one byte per voxel per step), 2 replays them, 0 stops."""
+        self._ck(self.f["set_decisions"](self.sim.h, mode, steps))
+
+    def decisions(self, steps: int) -> np.ndarray:
+        out = np.zeros((steps, self.sim.voxel_count()), np.uint8)
+        self._ck(self.f["get_decisions"](self.sim.h, _ptr(out, C.c_ubyte), steps))
+        return out
+
+    def put_decisions(self, rows: np.ndarray):
+        rows = np.ascontiguousarray(rows, np.uint8)
+        self._ck(self.f["put_decisions"](self.sim.h, _ptr(rows, C.c_ubyte), rows.shape[0]))
 
     def link_pipeline(self) -> int:
         out = np.zeros(1, np.int32)
