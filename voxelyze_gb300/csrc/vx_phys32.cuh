@@ -226,15 +226,15 @@ VX_HD float transverse_strain_sum_of(const vxg_voxel_material& m, const f3& ps, 
   }
 }
 
-// POIS: some voxel material has nu != 0 (otherwise no Poisson strain is ever read)
+// POIS: some voxel material has nu != 0 (otherwise no Poisson strain is ever read).
+// link_gather_own loads the link's own state and endpoint ids, link_gather_ends the rest (rest
+// length, endpoint poses, materials and Poisson caches).
 template <bool POIS>
-VX_HD LinkIn link_gather(const View& S, int l) {
+VX_HD void link_gather_own(const View& S, int l, LinkIn& in, int& vn, int& vp) {
   const vx64::View& B = S.B;
-  const int nl = B.nl, nv = B.nv;
-  LinkIn in;
+  const int nl = B.nl;
   in.lf = B.lflags[l];
   in.lmat = B.lmat[l];
-  in.rd = S.restDelta[l];
   in.oldPos2 = ld3(S.pos2, nl, l);
   // a small-angle link's angle1 is the identity, so its stored rotation vector is zero
   // (CVX_Link::orientLink, src/VX_Link.cpp:101-111; a new link starts small-angle with zeros, :63-68)
@@ -250,7 +250,14 @@ VX_HD LinkIn link_gather(const View& S, int l) {
   }
   in.maxStrain = B.maxStrain[l];
   in.strainOffset = B.strainOffset[l];
-  int vn = B.lvox[l], vp = B.lvox[nl + l];
+  vn = B.lvox[l];
+  vp = B.lvox[nl + l];
+}
+template <bool POIS>
+VX_HD void link_gather_ends(const View& S, int l, LinkIn& in, int vn, int vp) {
+  const vx64::View& B = S.B;
+  const int nv = B.nv;
+  in.rd = S.restDelta[l];
   in.dn = f3_of(S.P[vn]);
   in.dp = f3_of(S.P[vp]);
   in.qn = q4_of(S.Q[vn]);
@@ -263,6 +270,13 @@ VX_HD LinkIn link_gather(const View& S, int l) {
   } else {
     in.psn = in.psp = F3(0, 0, 0);
   }
+}
+template <bool POIS>
+VX_HD LinkIn link_gather(const View& S, int l) {
+  LinkIn in;
+  int vn, vp;
+  link_gather_own<POIS>(S, l, in, vn, vp);
+  link_gather_ends<POIS>(S, l, in, vn, vp);
   return in;
 }
 
@@ -411,15 +425,44 @@ VX_HD void kahan_add(float& sum, float& comp, float x) {
   sum = t;
 }
 
+// What the voxel pass reads of the voxel itself: written only by voxel passes and host uploads,
+// never by the link pass or the collision stage of the same step.
+struct VoxIn {
+  int vmat, ei;
+  uint32_t flags;
+  f3 d, c, lin, ang;
+  q4 q, qc;
+  int lk[6];
+  float temp;
+  int iz;
+};
+VX_HD void voxel_gather_own(const View& S, int v, VoxIn& in) {
+  const vx64::View& B = S.B;
+  const int nv = B.nv;
+  in.vmat = B.vmat[v];
+  in.ei = B.vext[v];
+  in.flags = B.vflags[v];
+  in.d = f3_of(S.P[v]);
+  in.c = ld3(S.c, nv, v);
+  in.lin = ld3(S.lin, nv, v);
+  in.ang = ld3(S.ang, nv, v);
+  in.q = q4_of(S.Q[v]);
+  in.qc = ldq(S.qc, nv, v);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) in.lk[i] = B.vlinks[i * nv + v];
+  in.temp = B.temp[v];
+  in.iz = B.vidx[2 * nv + v];
+}
+
 // FUSE_POIS: fill the Poisson-strain cache for the next step's link pass here, from this step's
 // link strains (which no later kernel of the step changes), instead of in a separate pre-pass
 template <bool FUSE_POIS>
-VX_HDN void voxel_update(const View& S, int v, float dt) {
+VX_HDN void voxel_step(const View& S, int v, float dt, const VoxIn& in) {
   const vx64::View& B = S.B;
   const int nv = B.nv, nl = B.nl;
   if (dt == 0.0f) return;
-  const vxg_voxel_material& m = B.vm[B.vmat[v]];
-  int ei = B.vext[v];
+  const vxg_voxel_material& m = B.vm[in.vmat];
+  int ei = in.ei;
   const vxg_external* e = ei >= 0 ? &B.ext[ei] : nullptr;
   if (e && (e->dof & 0x3F) == 0x3F) {
     S.P[v] = make_float4((float)e->translation[0], (float)e->translation[1], (float)e->translation[2], 0.0f);
@@ -430,12 +473,12 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
     st3(S.ang, nv, v, F3(0, 0, 0));
     return;
   }
-  uint32_t flags = B.vflags[v];
-  f3 d = f3_of(S.P[v]), c = ld3(S.c, nv, v), lin = ld3(S.lin, nv, v), ang = ld3(S.ang, nv, v);
-  q4 q = q4_of(S.Q[v]), qc = ldq(S.qc, nv, v);
+  const uint32_t flags = in.flags;
+  f3 d = in.d, c = in.c, lin = in.lin, ang = in.ang;
+  q4 q = in.q, qc = in.qc;
   int lk[6];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) lk[i] = B.vlinks[i * nv + v];
+  for (int i = 0; i < 6; ++i) lk[i] = in.lk[i];
   f3 F = F3(0, 0, 0);
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
@@ -466,8 +509,8 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
   bool floorOn = flags & VXG_VF_FLOOR;
   bool staticF = flags & VXG_VF_STATIC_FRICTION;
   // floor penetration: (base size - nominal)/2 - z, with z = iz s + d.z
-  float expand = m.sizeAvgF * (1 + B.temp[v] * m.alphaCTE) - m.nomSizeF;
-  float zorg = (float)B.vidx[2 * nv + v] * S.s;
+  float expand = m.sizeAvgF * (1 + in.temp * m.alphaCTE) - m.nomSizeF;
+  float zorg = (float)in.iz * S.s;
   float pen = (0.5f * expand - zorg) - (d.z - c.z);
   if (floorOn) {
     if (pen >= 0) {
@@ -571,6 +614,12 @@ VX_HDN void voxel_update(const View& S, int v, float dt) {
     }
   }
   if (nf != flags) B.vflags[v] = nf;  // the flags change rarely (friction latch, Poisson cache state)
+}
+template <bool FUSE_POIS>
+VX_HDN void voxel_update(const View& S, int v, float dt) {
+  VoxIn in;
+  voxel_gather_own(S, v, in);
+  voxel_step<FUSE_POIS>(S, v, dt, in);
 }
 
 }  // namespace vx32

@@ -367,9 +367,22 @@ int grid_for(int n) { return std::max(1, (n + kBlock - 1) / kBlock); }
 int grid_of(int n, int b) { return std::max(1, (n + b - 1) / b); }
 
 // ---- FP32C kernels ------------------------------------------------------------------------
+// Programmatic dependent launch between the passes of a step: a pass launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may start its blocks while the previous
+// kernel is still running.  Before pdl_wait a block reads only state that the previous kernel does
+// not write; pdl_wait returns once the previous kernel has finished and its writes are visible.  A
+// block lets the next pass launch (pdl_trigger) only after its own wait, so at most two kernels
+// overlap and everything before the previous kernel is complete.  Launched normally, the wait
+// returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 template <bool RECOMMEND, bool FORCES, bool POIS>
 __global__ void __launch_bounds__(512) k_link32(vx32::View S, int parity) {
   int l = blockIdx.x * blockDim.x + threadIdx.x;
+  // nothing is read before the wait (loading the link's own state ahead of it measured slower)
+  pdl_wait();
+  pdl_trigger();
   if (S.B.ctl->halt) return;
   float f2 = 0.0f;
   bool live = l < S.B.nl;
@@ -524,6 +537,12 @@ __global__ void __launch_bounds__(kLpT) k_link32p(vx32::View S, int ntiles) {
 template <bool RECOMMEND, bool FUSE_POIS>
 __global__ void __launch_bounds__(512) k_voxel32(vx32::View S, float dt_fixed, int parity, float fallback) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = v < S.B.nv;
+  vx32::VoxIn in;
+  // the voxel's own state: neither the link pass nor the collision stage writes it
+  if (live) vx32::voxel_gather_own(S, v, in);
+  pdl_wait();
+  pdl_trigger();
   if (S.B.ctl->halt) return;
   if (S.B.ctl->diverged) {
     if (v == 0) S.B.ctl->halt = 1;
@@ -536,8 +555,8 @@ __global__ void __launch_bounds__(512) k_voxel32(vx32::View S, float dt_fixed, i
     S.B.ctl->last_dt = dt;  // the next step's link pass reads it as every voxel's previous dt
     if (RECOMMEND) S.B.ctl->maxf[parity ^ 1] = 0u;
   }
-  if (v >= S.B.nv) return;
-  vx32::voxel_update<FUSE_POIS>(S, v, dt);
+  if (!live) return;
+  vx32::voxel_step<FUSE_POIS>(S, v, dt, in);
 }
 // FP64 interchange fields <-> FP32C working state, one field per launch (only the fields the host
 // writes are converted on upload, only the fields it reads on download)
@@ -771,6 +790,7 @@ struct vxg_engine {
   // the last step makes the next batch refill those caches first (k_poisson<true>)
   bool poisson_redo = true;
   bool poisson_fuse = true;  // vxg_set_poisson_fusion
+  bool pdl = true;           // FP32C passes launched to overlap the previous kernel's tail
   int* h_ctl = nullptr;      // pinned copy of the batch's control words
   // kernels launched by the time step (a graph replay counts the kernels it holds)
   long long n_launch = 0, graph_kernels = 0, cgraph_kernels = 0;
@@ -1350,6 +1370,24 @@ static void poisson_refill(vxg_engine* e) {
 
 // enqueue one step (no synchronisation); in timing mode `ev` holds this step's 4 events.  `first`:
 // the first step of a batch or of a captured chunk.
+// a launch that may overlap the previous kernel in the stream (the kernel waits for it itself)
+extern "C++" {
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(bool pdl, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+}
+
 static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEvent_t* ev = nullptr) {
   const View& S = e->S;
   bool rec = dt < 0;
@@ -1357,7 +1395,14 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   const int gl = grid_of(e->nl, bl), gv = grid_of(e->nv, bv);
   if (ev) pass_event(ev[0], e->stream);
   // kernels this step launches (or, under capture, records)
-  (void)first;
+  // overlap (launch_pdl) only where the kernel just before in the stream is known: a link pass
+  // (which reads nothing before its wait) right after the previous step's voxel pass, and a voxel
+  // pass right after its step's link pass (its early reads are the voxel's own state, which the
+  // link pass never writes).  Any other kernel in between (actuation, the Poisson pre-pass, the
+  // collision stage), a first step (conversions may precede it) or timing events make the launch
+  // an ordinary one.
+  const bool pdl_base = e->pdl && !ev && e->precision == VXG_FP32C;
+  bool link_pdl = pdl_base && !first && !e->act_mode;
   long long nk = 1 + (e->nl ? 1 : 0) + (e->act_mode && e->nv ? 1 + (e->nl ? 1 : 0) : 0) +
                  (e->g.any_poisson && e->nv && !fused_poisson(e) ? 1 : 0);
   if (e->act_mode && e->nv) {
@@ -1370,8 +1415,10 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   }
   // FP32C fills the cache in the voxel pass; caches the host invalidated are refilled before the
   // batch (poisson_refill), so no pre-pass runs inside it
-  if (e->g.any_poisson && e->nv && !fused_poisson(e))
+  if (e->g.any_poisson && e->nv && !fused_poisson(e)) {
     k_poisson<false><<<grid_for(e->nv), kBlock, 0, e->stream>>>(S);
+    link_pdl = false;
+  }
   if (e->precision == VXG_FP32C) {
     if (e->nl) {
       const bool pois = e->tab_poisson;
@@ -1384,20 +1431,21 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
         if (pois) k_link32p<true><<<grid, kLpT, kLpSmem, e->stream>>>(e->V, ntiles);
         else k_link32p<false><<<grid, kLpT, kLpSmem, e->stream>>>(e->V, ntiles);
       } else {
-        if (pois) k_link32<false, true, true><<<gl, bl, 0, e->stream>>>(e->V, parity);
-        else k_link32<false, true, false><<<gl, bl, 0, e->stream>>>(e->V, parity);
+        if (pois) launch_pdl(link_pdl, k_link32<false, true, true>, gl, bl, e->stream, e->V, parity);
+        else launch_pdl(link_pdl, k_link32<false, true, false>, gl, bl, e->stream, e->V, parity);
       }
     }
     if (ev) pass_event(ev[1], e->stream);
     if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream);
     if (ev) pass_event(ev[2], e->stream);
     e->n_launch += nk;
+    const bool voxel_pdl = pdl_base && e->nl && e->lp_bps == 0 && !e->g.collisions;
     if (fused_poisson(e)) {
       if (rec) k_voxel32<true, true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
-      else k_voxel32<false, true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+      else launch_pdl(voxel_pdl, k_voxel32<false, true>, gv, bv, e->stream, e->V, dt, parity, e->g.fallback_freq2);
     } else {
       if (rec) k_voxel32<true, false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
-      else k_voxel32<false, false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
+      else launch_pdl(voxel_pdl, k_voxel32<false, false>, gv, bv, e->stream, e->V, dt, parity, e->g.fallback_freq2);
     }
     if (ev) pass_event(ev[3], e->stream);
     return;
