@@ -76,7 +76,7 @@ def fp32c_bytes(n_voxels: int, n_links: int, poisson: bool, large_angle_links: i
 # 128x128x64 lattice, FP32C, warm step (profiles/fp32c_lattice128x128x64_dram.md), per unit
 MEASURED_TRAFFIC = {
     "fp32c_link": {"per_voxel": 0.0, "per_link": 135.5},    # k_link32
-    "fp32c_voxel": {"per_voxel": 330.7, "per_link": 0.0},   # k_voxel32 with the Poisson fill
+    "fp32c_voxel": {"per_voxel": 330.4, "per_link": 0.0},   # k_voxel32 with the Poisson fill
 }
 
 
