@@ -98,6 +98,9 @@ int vx_autotune(void* s, int trial_steps, float dt, int* out3);            /* vx
 int vx_set_link_pipeline(void* s, int blocks_per_sm);                      /* vxg_set_link_pipeline */
 int vx_get_link_pipeline(void* s, int* blocks_per_sm);                     /* vxg_get_link_pipeline */
 int vx_set_poisson_fusion(void* s, int on);                                /* vxg_set_poisson_fusion */
+/* the engine behind a handle (include/vxg.h), pending host edits uploaded first; NULL on failure.
+ * No counterpart in the reference: for callers that mix the engine ABI with this facade. */
+void* vx_engine(void* s);
 int vx_set_decisions(void* s, int mode, long long steps);                  /* vxg_set_decisions */
 int vx_get_decisions(void* s, unsigned char* out, long long steps);        /* vxg_get_decisions */
 int vx_put_decisions(void* s, const unsigned char* in, long long steps);   /* vxg_put_decisions */

@@ -149,6 +149,10 @@ int vxg_destroy(vxg_engine* e);
 int vxg_precision(const vxg_engine* e);
 /* (Re)allocates every device array for the given counts.  State is undefined until set. */
 int vxg_resize(vxg_engine* e, int n_voxels, int n_links);
+/* Index fields (voxel materials, externals and links, link voxels and materials) are checked on
+ * the device before the first kernel that dereferences them after an upload (vxg_step,
+ * vxg_recommended_dt, vxg_reduce, ...): an index out of range makes that call return VXG_E_ARG,
+ * naming the field and element, and nothing runs. */
 int vxg_set_field(vxg_engine* e, int field, const void* host, long long count);
 int vxg_get_field(vxg_engine* e, int field, void* host, long long count);
 int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const vxg_link_material* lm,

@@ -1529,6 +1529,10 @@ int vx_set_poisson_fusion(void* s, int on) {
   if (!vx.upload()) return -1;
   return vxg_set_poisson_fusion(vx.impl()->eng, on) ? -1 : 0;
 }
+void* vx_engine(void* s) {
+  CVoxelyze& vx = H(s)->vx;
+  return vx.upload() ? (void*)vx.impl()->eng : nullptr;
+}
 int vx_set_decisions(void* s, int mode, long long steps) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.upload()) return -1;

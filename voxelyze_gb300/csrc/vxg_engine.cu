@@ -14,6 +14,7 @@
 // captured CUDA graph.  Nothing is synchronised inside a batch; the host reads the control block
 // once per batch.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cstddef>
@@ -361,6 +362,35 @@ __global__ void k_reduce_fixed(View S, int info, int n, int type, double* scratc
   *out = type == 0 ? (float)a : type == 1 ? (float)b : type == 2 ? (float)c : (float)(c / n);
   *done = 0u;
   __threadfence();
+}
+
+// Every index the step kernels dereference, checked on the device once per upload of topology or
+// tables: a bad value becomes an error return instead of an out-of-bounds access.  Records the
+// smallest (field << 32 | element) found; reads only the index arrays themselves, in bounds.
+enum { VAL_VMAT = 1, VAL_VEXT, VAL_VLINKS, VAL_LVOX, VAL_LMAT, VAL_POWSLOT };
+__global__ void k_validate(View S, int n_vm, int n_lm, int n_ext, int n_powslots, unsigned long long* bad) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = S.nv, nl = S.nl;
+  auto flag = [&](int field, long long el) { atomicMin(bad, ((unsigned long long)field << 32) | (unsigned long long)el); };
+  if (i < nv) {
+    const int m = S.vmat[i], x = S.vext[i];
+    if (m < 0 || m >= n_vm) flag(VAL_VMAT, i);
+    if (x < -1 || x >= n_ext) flag(VAL_VEXT, i);
+    for (int k = 0; k < 6; ++k) {
+      const int l = S.vlinks[(size_t)k * nv + i];
+      if (l < -1 || l >= nl) flag(VAL_VLINKS, (long long)k * nv + i);
+    }
+  }
+  if (i < nl) {
+    const int a = S.lvox[i], b = S.lvox[(size_t)nl + i], m = S.lmat[i];
+    if (a < 0 || a >= nv) flag(VAL_LVOX, i);
+    if (b < 0 || b >= nv) flag(VAL_LVOX, (long long)nl + i);
+    if (m < 0 || m >= n_lm) flag(VAL_LMAT, i);
+  }
+  if (i < n_vm) {
+    const int ps = S.vm[i].powf_slot;
+    if (ps < -1 || ps >= n_powslots) flag(VAL_POWSLOT, i);
+  }
 }
 
 int grid_for(int n) { return std::max(1, (n + kBlock - 1) / kBlock); }
@@ -791,6 +821,8 @@ struct vxg_engine {
   bool poisson_redo = true;
   bool poisson_fuse = true;  // vxg_set_poisson_fusion
   bool pdl = true;           // FP32C passes launched to overlap the previous kernel's tail
+  bool topo_ok = false;      // k_validate passed for the current index fields and tables
+  unsigned long long* d_bad = nullptr;
   int* h_ctl = nullptr;      // pinned copy of the batch's control words
   // kernels launched by the time step (a graph replay counts the kernels it holds)
   long long n_launch = 0, graph_kernels = 0, cgraph_kernels = 0;
@@ -897,6 +929,7 @@ static void rebuild_view(vxg_engine* e) {
   e->V.s = (float)e->g.voxSize;
   if (e->precision == VXG_FP32C) e->col.bind32(e->V);
   e->graph_valid = false;
+  e->topo_ok = false;
 }
 
 static bool is_state_field(int f) {
@@ -972,6 +1005,10 @@ __attribute__((visibility("hidden"))) int vxg_reduce_fixed(vxg_engine* e, int in
   if (info == 8) {
     *why = "vx_state_info_into: PRESSURE is reduced on the host";
     return VXG_E_ARG;
+  }
+  if (!e->topo_ok) {  // checking the index fields would allocate: a step checks them
+    *why = "vx_state_info_into: the scene's indices are not checked yet (step first)";
+    return VXG_E_STATE;
   }
   const bool link = info == 5 || info == 6 || info == 7;
   const long long n = link ? e->nl : e->nv;
@@ -1056,6 +1093,7 @@ int vxg_destroy(vxg_engine* e) {
   if (e->d_sp_idx) cudaFree(e->d_sp_idx);
   if (e->d_sp_t) cudaFree(e->d_sp_t);
   if (e->d_dec) cudaFree(e->d_dec);
+  if (e->d_bad) cudaFree(e->d_bad);
   for (void* p : {(void*)e->d_mesh_vv, (void*)e->d_mesh_quads, (void*)e->d_mesh_vert, (void*)e->d_mesh_norm})
     if (p) cudaFree(p);
   if (e->d_partials) cudaFree(e->d_partials);
@@ -1128,6 +1166,9 @@ int vxg_set_field(vxg_engine* e, int f, const void* host, long long count) {
   if (count != n) return fail(e, VXG_E_SIZE, "vxg_set_field: element count mismatch");
   if (n == 0) return VXG_OK;
   e->poisson_redo = true;
+  if (f == VXG_F_VOXEL_MATERIAL || f == VXG_F_VOXEL_LINKS || f == VXG_F_VOXEL_EXTERNAL ||
+      f == VXG_F_LINK_VOXELS || f == VXG_F_LINK_MATERIAL)
+    e->topo_ok = false;
   if (e->precision == VXG_FP32C && is_state_field(f)) {
     e->dirty64 |= 1u << f;   // the FP64 copy is now the newer one
     e->stale64 &= ~(1u << f);
@@ -1266,9 +1307,17 @@ int vxg_mesh_topology(vxg_engine* e, int n_vertices, const int* vertex_voxels, i
   return VXG_OK;
 }
 
+static int check_topology(vxg_engine* e);
+// an NVTX range for the length of a scope (named in profiler timelines; free without a profiler)
+struct NvtxScope {
+  explicit NvtxScope(const char* name) { nvtxRangePushA(name); }
+  ~NvtxScope() { nvtxRangePop(); }
+};
 int vxg_mesh_update(vxg_engine* e, float* vertices, float* normals) {
+  NvtxScope nvtx("vxg_mesh_update");
   if (!e) return VXG_E_ARG;
   VXG_CK(cudaSetDevice(e->device));
+  if (int rc = check_topology(e)) return rc;
   ensure32(e);  // FP32C: host-written state first
   const int nvt = e->n_mesh_vert, nq = e->n_mesh_quad;
   if (nvt) {
@@ -1326,6 +1375,11 @@ int vxg_set_globals(vxg_engine* e, const vxg_globals* g) {
 
 int vxg_set_nearby(vxg_engine* e, const int* offsets, const int* items, long long n_items) {
   if (!e || !offsets || (n_items > 0 && !items)) return VXG_E_ARG;
+  if (offsets[0] != 0 || offsets[e->nv] != n_items) return fail(e, VXG_E_ARG, "vxg_set_nearby: offsets do not span the items");
+  for (int v = 0; v < e->nv; ++v)
+    if (offsets[v + 1] < offsets[v]) return fail(e, VXG_E_ARG, "vxg_set_nearby: offsets decrease");
+  for (long long k = 0; k < n_items; ++k)
+    if (items[k] < 0 || items[k] >= e->nv) return fail(e, VXG_E_ARG, "vxg_set_nearby: voxel index out of range");
   VXG_CK(cudaSetDevice(e->device));
   int rc = e->col.set_nearby(e->nv, offsets, items, n_items, e->stream);
   if (rc) return fail(e, rc, "nearby upload");
@@ -1370,6 +1424,29 @@ static void poisson_refill(vxg_engine* e) {
 
 // enqueue one step (no synchronisation); in timing mode `ev` holds this step's 4 events.  `first`:
 // the first step of a batch or of a captured chunk.
+// k_validate once per change of the index fields or tables, before any kernel dereferences them
+static const char* const kValField[] = {"", "voxel material", "voxel external", "voxel link", "link voxel",
+                                        "link material", "material powf slot"};
+static int check_topology(vxg_engine* e) {
+  if (e->topo_ok) return VXG_OK;
+  if (!e->d_bad) VXG_CK(cudaMalloc(&e->d_bad, sizeof(unsigned long long)));
+  unsigned long long none = ~0ull, bad = 0;
+  VXG_CK(cudaMemcpyAsync(e->d_bad, &none, sizeof(none), cudaMemcpyHostToDevice, e->stream));
+  const int n = std::max(std::max(e->nv, e->nl), e->n_vm);
+  if (n > 0) k_validate<<<grid_for(n), kBlock, 0, e->stream>>>(e->S, e->n_vm, e->n_lm, e->n_ext, e->n_powslots, e->d_bad);
+  VXG_CK(cudaMemcpyAsync(&bad, e->d_bad, sizeof(bad), cudaMemcpyDeviceToHost, e->stream));
+  VXG_CK(cudaStreamSynchronize(e->stream));
+  if (bad != ~0ull) {
+    char msg[160];
+    const int field = (int)(bad >> 32);
+    snprintf(msg, sizeof msg, "index out of range: %s, element %llu", field > 0 && field < 7 ? kValField[field] : "?",
+             bad & 0xffffffffull);
+    return fail(e, VXG_E_ARG, msg);
+  }
+  e->topo_ok = true;
+  return VXG_OK;
+}
+
 // a launch that may overlap the previous kernel in the stream (the kernel waits for it itself)
 extern "C++" {
 template <typename... KArgs, typename... Args>
@@ -1493,6 +1570,7 @@ static int capture(vxg_engine* e, int n, float dt, cudaGraphExec_t* out) {
 }
 
 int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged) {
+  NvtxScope nvtx("vxg_step");
   if (!e || nsteps < 0) return VXG_E_ARG;
   if (!e->have_globals) return fail(e, VXG_E_STATE, "vxg_set_globals was not called");
   if (steps_done) *steps_done = 0;
@@ -1503,6 +1581,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   }
   if (e->act_mode == 2 && e->n_phase < e->nv) return fail(e, VXG_E_STATE, "actuation phases cover fewer voxels than the scene");
   VXG_CK(cudaSetDevice(e->device));
+  if (int rc = check_topology(e)) return rc;
   ensure32(e);
   if (e->precision == VXG_FP32C) e->stale64 = all_state_bits();
   // reset the per-batch control words: diverged, halt, steps, status and the dt maxima (keep time
@@ -1604,6 +1683,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
 // ---- differentiated run ---------------------------------------------------------------------
 int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every, const int* body_offsets,
                       int n_bodies, double* objective, double* dE, double* drho, double* dphase) {
+  NvtxScope nvtx("vxg_adjoint_com_x");
   if (!e || nsteps <= 0 || !(dt > 0.0f) || checkpoint_every <= 0 || !body_offsets || n_bodies <= 0 || !objective)
     return VXG_E_ARG;
   if (!e->have_globals) return fail(e, VXG_E_STATE, "vxg_set_globals was not called");
@@ -1616,6 +1696,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
     if (body_offsets[b] < 0 || body_offsets[b + 1] < body_offsets[b] || body_offsets[b + 1] > e->nv)
       return fail(e, VXG_E_ARG, "vxg_adjoint_com_x: body offsets out of range");
   VXG_CK(cudaSetDevice(e->device));
+  if (int rc = check_topology(e)) return rc;
   const int nv = e->nv, nl = e->nl, K = std::min(checkpoint_every, nsteps);
   const int nck = (nsteps + K - 1) / K;
   const size_t ckb = e->arena_bytes + sizeof(Ctl);
@@ -1704,9 +1785,11 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
 }
 
 int vxg_recommended_dt(vxg_engine* e, float* dt) {
+  NvtxScope nvtx("vxg_recommended_dt");
   if (!e || !dt) return VXG_E_ARG;
   if (!e->have_globals) return fail(e, VXG_E_STATE, "vxg_set_globals was not called");
   VXG_CK(cudaSetDevice(e->device));
+  if (int rc = check_topology(e)) return rc;
   int zeros[4] = {0, 0, 0, 0};
   VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
   unsigned z = 0u;
@@ -1764,6 +1847,7 @@ int vxg_set_temperatures(vxg_engine* e, const float* t) {
 int vxg_reduce(vxg_engine* e, int info, int type, float* out) {
   if (!e || !out || info < 0 || info > 9 || type < 0 || type > 3) return VXG_E_ARG;
   VXG_CK(cudaSetDevice(e->device));
+  if (int rc = check_topology(e)) return rc;
   bool link = info == 5 || info == 6 || info == 7;
   int n = link ? e->nl : e->nv;
   if (n == 0) { *out = 0.0f; return VXG_OK; }
@@ -1813,6 +1897,7 @@ int vxg_body_com(vxg_engine* e, const int* offsets, int n_bodies, double* out) {
   if (!e || !offsets || !out || n_bodies <= 0) return VXG_E_ARG;
   if (offsets[0] < 0 || offsets[n_bodies] > e->nv) return fail(e, VXG_E_SIZE, "vxg_body_com: offsets out of range");
   VXG_CK(cudaSetDevice(e->device));
+  if (int rc = check_topology(e)) return rc;
   if (n_bodies > e->n_body_cap) {
     if (e->d_body_off) cudaFree(e->d_body_off);
     if (e->d_body_out) cudaFree(e->d_body_out);
@@ -1953,6 +2038,7 @@ int vxg_restore(vxg_engine* e, int slot) {
 // Picks the link and voxel block sizes and the graph chunk length by timing short runs on the
 // current scene; the state is snapshotted before and restored after, so the simulation is unchanged.
 int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* best_voxel, int* best_chunk) {
+  NvtxScope nvtx("vxg_autotune");
   if (!e || trial_steps < 2) return VXG_E_ARG;
   const int slot = 1023;
   int rc = vxg_snapshot(e, slot);
