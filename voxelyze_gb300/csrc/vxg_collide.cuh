@@ -101,14 +101,19 @@ __device__ __forceinline__ double cpos(const ColView& C, int v, int k) {
   return C.vidx[k * C.nv + v] * C.s64 + ((double)d - (double)C.c32[k * C.nv + v]);
 }
 
+// one store of the stale word per block (a falling body moves most voxels past the threshold at
+// once, and a store from each of their warps to one address would serialise)
 __global__ void c_check(ColView C) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (C.ctl->halt || C.ctl->diverged) return;
+  if (C.ctl->halt || C.ctl->diverged) return;  // the same for the whole launch
   if (v == 0 && C.cc->force_stale) C.cc->stale = 1;
-  if (v >= C.nv || !is_surface(C, v)) return;
-  double dx = cpos(C, v, 0) - C.lastWatch[v], dy = cpos(C, v, 1) - C.lastWatch[C.nv + v],
-         dz = cpos(C, v, 2) - C.lastWatch[2 * C.nv + v];
-  if (dx * dx + dy * dy + dz * dz > C.recalc2) C.cc->stale = 1;
+  bool moved = false;
+  if (v < C.nv && is_surface(C, v)) {
+    double dx = cpos(C, v, 0) - C.lastWatch[v], dy = cpos(C, v, 1) - C.lastWatch[C.nv + v],
+           dz = cpos(C, v, 2) - C.lastWatch[2 * C.nv + v];
+    moved = dx * dx + dy * dy + dz * dz > C.recalc2;
+  }
+  if (__syncthreads_or(moved) && threadIdx.x == 0) C.cc->stale = 1;
 }
 
 // rebuild only when c_check found the list stale and the step has not diverged (the same for
