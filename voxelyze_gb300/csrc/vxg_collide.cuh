@@ -103,17 +103,18 @@ __device__ __forceinline__ double cpos(const ColView& C, int v, int k) {
 
 // one store of the stale word per block (a falling body moves most voxels past the threshold at
 // once, and a store from each of their warps to one address would serialise)
+// whether surface voxel v moved more than the rebuild distance since the last rebuild
+__device__ __forceinline__ bool c_moved(const ColView& C, int v) {
+  if (v >= C.nv || !is_surface(C, v)) return false;
+  double dx = cpos(C, v, 0) - C.lastWatch[v], dy = cpos(C, v, 1) - C.lastWatch[C.nv + v],
+         dz = cpos(C, v, 2) - C.lastWatch[2 * C.nv + v];
+  return dx * dx + dy * dy + dz * dz > C.recalc2;
+}
 __global__ void c_check(ColView C) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (C.ctl->halt || C.ctl->diverged) return;  // the same for the whole launch
   if (v == 0 && C.cc->force_stale) C.cc->stale = 1;
-  bool moved = false;
-  if (v < C.nv && is_surface(C, v)) {
-    double dx = cpos(C, v, 0) - C.lastWatch[v], dy = cpos(C, v, 1) - C.lastWatch[C.nv + v],
-           dz = cpos(C, v, 2) - C.lastWatch[2 * C.nv + v];
-    moved = dx * dx + dy * dy + dz * dz > C.recalc2;
-  }
-  if (__syncthreads_or(moved) && threadIdx.x == 0) C.cc->stale = 1;
+  if (__syncthreads_or(c_moved(C, v)) && threadIdx.x == 0) C.cc->stale = 1;
 }
 
 // rebuild only when c_check found the list stale and the step has not diverged (the same for
@@ -396,9 +397,9 @@ __device__ void c_contact32(const ColView& C, int c, int a, int b) {
 // CVX_Collision::updateContactForce  VX_Collision.cpp:42-56, one pair per thread of a resident grid
 // (the pair count is known only on the device)
 __device__ __forceinline__ void c_contact64(const ColView& C, int c, int a, int b);
-__global__ void c_contact(ColView C) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (C.ctl->halt || C.ctl->diverged) return;
+// the contact forces of every listed pair, thread t of `threads`; thread 0 also closes the step's
+// bookkeeping (rebuild count, stale words, status to the control block)
+__device__ __forceinline__ void c_contact_all(const ColView& C, int t, int threads) {
   const int npairs = C.cc->npairs, status = C.cc->status;  // thread 0 clears neither
   if (t == 0) {
     if (C.cc->stale) C.cc->rebuilds += 1;
@@ -407,11 +408,47 @@ __global__ void c_contact(ColView C) {
     if (status) atomicOr(&C.ctl->status, status << 8);
   }
   if (status) return;
-  for (int c = t; c < npairs; c += gridDim.x * blockDim.x) {
+  for (int c = t; c < npairs; c += threads) {
     int a = C.pairI[c], b = C.pairJ[c];
     if (C.fp32) c_contact32(C, c, a, b);
     else c_contact64(C, c, a, b);
   }
+}
+__global__ void c_contact(ColView C) {
+  if (C.ctl->halt || C.ctl->diverged) return;
+  c_contact_all(C, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// The whole stage in one cooperative launch: the stale test, the rebuild phases when it found the
+// list stale, the contact forces, separated by grid-wide barriers (a cooperative launch keeps
+// every block resident, so the barriers end; every branch around a barrier reads words that
+// were written before the previous barrier, so all blocks take it alike).
+__global__ void __launch_bounds__(256) c_stage(ColView C) {
+  if (C.ctl->halt || C.ctl->diverged) return;  // uniform: set before this launch
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  bool moved = false;
+  for (int v = first; v < C.nv; v += stride) moved |= c_moved(C, v);
+  if (first == 0 && C.cc->force_stale) C.cc->stale = 1;
+  if (__syncthreads_or(moved) && threadIdx.x == 0) C.cc->stale = 1;
+  grid.sync();
+  if (C.cc->stale) {
+    c_clear_range(C, first, stride);
+    grid.sync();
+    for (int v = first; v < C.nv; v += stride) c_insert_one(C, v);
+    grid.sync();
+    for (int v = first; v < C.nv; v += stride) c_count_one(C, v);
+    grid.sync();
+    if (blockIdx.x == 0) c_scan_block(C);
+    grid.sync();
+    if (!C.cc->status)
+      for (int v = first; v < C.nv; v += stride) c_fill_one(C, v);
+    grid.sync();
+    if (!C.cc->status)
+      for (int v = first; v < C.nv; v += stride) c_watch_one(C, v);
+    grid.sync();
+  }
+  c_contact_all(C, first, stride);
 }
 __device__ __forceinline__ void c_contact64(const ColView& C, int c, int a, int b) {
   const int nv = C.nv;
@@ -470,6 +507,7 @@ struct Collide {
     C.pairForce = nullptr;
     nv = n;
     coop_blocks = -1;
+    stage_blocks = -1;
     if (!cc) {
       if (cudaMalloc(&cc, sizeof(ColCtl)) != cudaSuccess) return VXG_E_CUDA;
     }
@@ -610,9 +648,32 @@ struct Collide {
   // Launches the stage on stream s; returns the number of kernels launched.  The rebuild exits at
   // once unless c_check found the pair list stale.  (A conditional graph node around separate
   // rebuild kernels measured slower than their early exits on GB300.)
+  // the whole stage as one cooperative launch: blocks resident on the whole GPU (0: not available)
+  int stage_blocks = -1;
+  int stage_grid() {
+    if (stage_blocks < 0) {
+      int dev = 0, n_sm = 1, coop = 0, per_sm = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+      if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c_stage, 256, 0) == cudaSuccess && per_sm > 0)
+        stage_blocks = std::min(n_sm * per_sm, std::max(1, (nv + 255) / 256));
+      else
+        stage_blocks = 0;
+      cudaGetLastError();
+    }
+    return stage_blocks;
+  }
   int enqueue(const vxg_globals& g, cudaStream_t s) {
     if (!buf || !C.nbOff) return 0;
     set_globals(g);
+    const int gs = stage_grid();
+    if (gs > 0) {
+      void* args[] = {&C};
+      if (cudaLaunchCooperativeKernel((const void*)c_stage, dim3(gs), dim3(256), args, 0, s) == cudaSuccess) return 1;
+      cudaGetLastError();
+      stage_blocks = 0;  // not available here: the separate kernels from now on
+    }
     int gv = std::max(1, (nv + 255) / 256);
     c_check<<<gv, 256, 0, s>>>(C);
     int n = enqueue_rebuild(s);
