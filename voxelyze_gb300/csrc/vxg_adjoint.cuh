@@ -30,6 +30,7 @@ struct AdjBuf {
   double* tl;           // K x 9 nl: pos2 3, angle1v 3, angle2v 3
   uint32_t* tlf;        // K x nl link flags
   float* ttime;         // K step start times
+  float* ttemp;         // K x nv temperatures each step used (after its actuation)
   double* lam;          // 13 nv adjoint of the voxel state
   double* gFM;          // 6 nv adjoint of the summed link force (3) and moment (3), voxel frame
   double* mu;           // 9 nl adjoint of the link pose (pos2, angle1v, angle2v)
@@ -43,15 +44,15 @@ struct AdjBuf {
   int* err;             // bit 0: a link left the small-angle branch
 };
 
-__device__ __forceinline__ float act_temp(const View& S, const ActParams& A, int v, float time) {
-  if (A.mode == 0) return S.temp[v];
-  double arg = 2.0 * 3.141592653589793 * A.freq * (double)time + (A.phase ? (double)A.phase[v] : 0.0);
-  int f = 0;
-  return (float)(A.amp * vxm::cr_sin(arg, &f));
-}
 __device__ __forceinline__ double act_dtemp_dphase(const ActParams& A, int v, float time) {
   double arg = 2.0 * 3.141592653589793 * A.freq * (double)time + (A.phase ? (double)A.phase[v] : 0.0);
   return A.amp * cos(arg);
+}
+
+// the temperatures step `slot` used: launched right after the step, before the next actuation
+__global__ void k_tape_temp(View S, AdjBuf T, int slot) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < S.nv) T.ttemp[(size_t)slot * S.nv + i] = S.temp[i];
 }
 
 __global__ void k_tape_save(View S, AdjBuf T, int slot) {
@@ -100,8 +101,8 @@ __device__ vxa::LinkIn tape_link_in(const View& S, const AdjBuf& T, const ActPar
   const vxg_voxel_material& mn = S.vm[S.vmat[vn]];
   const vxg_voxel_material& mp = S.vm[S.vmat[vp]];
   if (A.mode) {  // CVX_Link::updateRestLength after the step's setTemperature (VX_Link.cpp:137-140)
-    float time = T.ttime[slot];
-    float tn = act_temp(S, A, vn, time), tp = act_temp(S, A, vp, time);
+    const float* tt = T.ttemp + (size_t)slot * nv;
+    float tn = tt[vn], tp = tt[vp];
     in.rest = 0.5 * (mn.size[in.axis] * (1 + tn * mn.alphaCTE) + mp.size[in.axis] * (1 + tp * mp.alphaCTE));
   } else {
     in.rest = S.rest[l];
@@ -171,7 +172,7 @@ __global__ void k_adj_voxel(View S, AdjBuf T, ActParams A, int slot, float dt) {
   in.c2xSqMxExS = m.c2xSqMxExS; in.c2xSqIxExSxSxS = m.c2xSqIxExSxSxS;
   in.zetaGlobal = m.zetaGlobal; in.zetaCollision = m.zetaCollision; in.gravMult = m.gravMult;
   in.penetrationStiffness = m.penetrationStiffness; in.muStatic = m.muStatic; in.muKinetic = m.muKinetic;
-  float temp = act_temp(S, A, v, T.ttime[slot]);
+  float temp = T.ttemp[(size_t)slot * nv + v];
   {  // CVX_Voxel::baseSizeAverage (VX_Voxel.h:90) at this step's temperature
     float f = 1 + temp * m.alphaCTE;
     double bsa = ((double)f * m.size[0] + (double)f * m.size[1] + (double)f * m.size[2]) / 3.0f;

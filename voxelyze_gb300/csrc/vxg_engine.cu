@@ -1706,6 +1706,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   size_t o_tv = carve(sizeof(double) * 13 * (size_t)nv * K), o_tvf = carve(sizeof(uint32_t) * (size_t)nv * K),
          o_tpd = carve(sizeof(float) * (size_t)nv * K), o_tl = carve(sizeof(double) * 9 * (size_t)nl * K),
          o_tlf = carve(sizeof(uint32_t) * (size_t)nl * K), o_tt = carve(sizeof(float) * K),
+         o_ttemp = carve(sizeof(float) * (size_t)nv * K),
          o_lam = carve(sizeof(double) * 13 * (size_t)nv), o_gfm = carve(sizeof(double) * 6 * (size_t)nv),
          o_mu = carve(sizeof(double) * 9 * (size_t)nl), o_lcon = carve(sizeof(double) * 14 * (size_t)nl),
          o_lpar = carve(sizeof(double) * 4 * (size_t)nl), o_lf = carve(sizeof(double) * 12 * (size_t)nl),
@@ -1719,6 +1720,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   T.K = K;
   T.tv = (double*)(buf + o_tv); T.tvf = (uint32_t*)(buf + o_tvf); T.tpd = (float*)(buf + o_tpd);
   T.tl = (double*)(buf + o_tl); T.tlf = (uint32_t*)(buf + o_tlf); T.ttime = (float*)(buf + o_tt);
+  T.ttemp = (float*)(buf + o_ttemp);
   T.lam = (double*)(buf + o_lam); T.gFM = (double*)(buf + o_gfm); T.mu = (double*)(buf + o_mu);
   T.lcon = (double*)(buf + o_lcon); T.lpar = (double*)(buf + o_lpar); T.lforce = (double*)(buf + o_lf);
   T.gTempV = (double*)(buf + o_gt);
@@ -1762,6 +1764,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
     for (int s = 0; s < n; ++s) {
       k_tape_save<<<gboth, kBlock, 0, e->stream>>>(e->S, T, s);
       enqueue_step(e, dt, s & 1, s == 0);
+      k_tape_temp<<<gvx, kBlock, 0, e->stream>>>(e->S, T, s);
     }
     for (int s = n - 1; s >= 0; --s) {
       if (nl) k_adj_link_forces<<<glk, kBlock, 0, e->stream>>>(e->S, T, A, s);
