@@ -679,8 +679,19 @@ __global__ void k_actuate(View S, double amp, double freq, const float* phase, i
   if (fp32) {
     t = (float)amp * sinf((float)arg);
   } else {
-    int f = 0;
-    t = (float)(amp * vxm::cr_sin(arg, &f));
+    // Ziv's rounding test: only the float result is kept.  The library sine is within a few ulp of
+    // sin(arg), so amp * sin(arg) lies within 2^-45 (relative) of y; when that whole interval
+    // rounds to one float, it is the float the correctly rounded sine gives.  Otherwise (about one
+    // value in four million), and for y == 0, evaluate the correctly rounded sine.
+    const double y = amp * sin(arg);
+    const double d = fabs(y) * 0x1p-45;
+    const float lo = __double2float_rn(y - d), hi = __double2float_rn(y + d);
+    if (y != 0.0 && lo == hi) {
+      t = lo;
+    } else {
+      int f = 0;
+      t = (float)(amp * vxm::cr_sin(arg, &f));
+    }
   }
   S.temp[v] = t;
 }
