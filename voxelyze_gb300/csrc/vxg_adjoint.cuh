@@ -31,6 +31,7 @@ struct AdjBuf {
   uint32_t* tlf;        // K x nl link flags
   float* ttime;         // K step start times
   float* ttemp;         // K x nv temperatures each step used (after its actuation)
+  double* tforce;       // K x 12 nl link forces and moments of each step (null: recomputed)
   double* lam;          // 13 nv adjoint of the voxel state
   double* gFM;          // 6 nv adjoint of the summed link force (3) and moment (3), voxel frame
   double* mu;           // 9 nl adjoint of the link pose (pos2, angle1v, angle2v)
@@ -49,10 +50,22 @@ __device__ __forceinline__ double act_dtemp_dphase(const ActParams& A, int v, fl
   return A.amp * cos(arg);
 }
 
-// the temperatures step `slot` used: launched right after the step, before the next actuation
-__global__ void k_tape_temp(View S, AdjBuf T, int slot) {
+// what step `slot` computed and the reverse sweep reads: the temperatures it used and, when the
+// tape has room, its link forces and moments (the layout k_adj_link_forces writes); launched right
+// after the step, before the next actuation or link pass
+__global__ void k_tape_step(View S, AdjBuf T, int slot) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < S.nv) T.ttemp[(size_t)slot * S.nv + i] = S.temp[i];
+  const int nv = S.nv, nl = S.nl;
+  if (i < nv) T.ttemp[(size_t)slot * nv + i] = S.temp[i];
+  if (T.tforce && i < nl) {
+    double* tf = T.tforce + (size_t)slot * 12 * nl;
+    for (int c = 0; c < 3; ++c) {
+      tf[(size_t)c * nl + i] = S.fN[(size_t)c * nl + i];
+      tf[(size_t)(3 + c) * nl + i] = S.fP[(size_t)c * nl + i];
+      tf[(size_t)(6 + c) * nl + i] = S.mN[(size_t)c * nl + i];
+      tf[(size_t)(9 + c) * nl + i] = S.mP[(size_t)c * nl + i];
+    }
+  }
 }
 
 __global__ void k_tape_save(View S, AdjBuf T, int slot) {

@@ -1724,6 +1724,16 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
          o_gt = carve(sizeof(double) * nv), o_acc = carve(sizeof(double) * 3 * (size_t)nv),
          o_err = carve(sizeof(int)), o_off = carve(sizeof(int) * ((size_t)n_bodies + 1)),
          o_obj = carve(sizeof(double) * n_bodies);
+  // the segment's link forces, taped when they fit in three quarters of the free memory (otherwise
+  // each reverse step recomputes them)
+  size_t o_tf = 0;
+  {
+    size_t free_b = 0, total_b = 0;
+    const size_t need = sizeof(double) * 12 * (size_t)nl * K;
+    if (nl && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && sz + need + 256 < free_b / 4 * 3)
+      o_tf = carve(need);
+    cudaGetLastError();
+  }
   char* buf = nullptr;
   VXG_CK(cudaMalloc(&buf, sz));
   struct Free { char* p; ~Free() { if (p) cudaFree(p); } } guard{buf};
@@ -1732,6 +1742,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   T.tv = (double*)(buf + o_tv); T.tvf = (uint32_t*)(buf + o_tvf); T.tpd = (float*)(buf + o_tpd);
   T.tl = (double*)(buf + o_tl); T.tlf = (uint32_t*)(buf + o_tlf); T.ttime = (float*)(buf + o_tt);
   T.ttemp = (float*)(buf + o_ttemp);
+  T.tforce = o_tf ? (double*)(buf + o_tf) : nullptr;
   T.lam = (double*)(buf + o_lam); T.gFM = (double*)(buf + o_gfm); T.mu = (double*)(buf + o_mu);
   T.lcon = (double*)(buf + o_lcon); T.lpar = (double*)(buf + o_lpar); T.lforce = (double*)(buf + o_lf);
   T.gTempV = (double*)(buf + o_gt);
@@ -1775,11 +1786,13 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
     for (int s = 0; s < n; ++s) {
       k_tape_save<<<gboth, kBlock, 0, e->stream>>>(e->S, T, s);
       enqueue_step(e, dt, s & 1, s == 0);
-      k_tape_temp<<<gvx, kBlock, 0, e->stream>>>(e->S, T, s);
+      k_tape_step<<<gboth, kBlock, 0, e->stream>>>(e->S, T, s);
     }
     for (int s = n - 1; s >= 0; --s) {
-      if (nl) k_adj_link_forces<<<glk, kBlock, 0, e->stream>>>(e->S, T, A, s);
-      k_adj_voxel<<<gvx, kBlock, 0, e->stream>>>(e->S, T, A, s, dt);
+      AdjBuf Ts = T;
+      if (T.tforce) Ts.lforce = T.tforce + (size_t)s * 12 * nl;  // taped by the recomputation
+      else if (nl) k_adj_link_forces<<<glk, kBlock, 0, e->stream>>>(e->S, T, A, s);
+      k_adj_voxel<<<gvx, kBlock, 0, e->stream>>>(e->S, Ts, A, s, dt);
       if (nl) k_adj_link<<<glk, kBlock, 0, e->stream>>>(e->S, T, A, s);
       k_adj_gather<<<gvx, kBlock, 0, e->stream>>>(e->S, T, A, s);
     }
