@@ -1,4 +1,4 @@
-"""Host edits between steps, the reference's way (SURVEY H5): per-voxel CVX_Voxel::setTemperature
+"""Host edits between steps, the reference's way: per-voxel CVX_Voxel::setTemperature
 and CVX_External setters called between doTimeStep calls (src/VX_Voxel.cpp:108-114,
 include/VX_External.h:39-90).  While the device holds the newer state the product queues the
 temperatures and applies them on the device before the next step or host read, and uploads only

@@ -1,4 +1,4 @@
-"""Topology edits between steps (SURVEY §8f row 2): setVoxel over an existing voxel (material
+"""Topology edits between steps: setVoxel over an existing voxel (material
 replacement), setVoxel(NULL) (removal), replaceMaterial, removeMaterial and setVoxelSize
 (src/Voxelyze.cpp:384-498, 541-575, 643-668).  Each edit renumbers voxels or links the way the
 reference's lists do (removal shifts later entries down; a replaced voxel's links move to the end
