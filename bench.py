@@ -390,7 +390,13 @@ def run_ours(args, world, rank, local):
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": b[kernel], "ms_per_launch": k_ms, "traffic": traffic,
             "step_bytes": b["step"], "step_frac": b["step"] / (t_head["total_ms"] / args.steps / 1e3) / 1e9 / peak,
-            "large_angle_links": large}
+            "large_angle_links": large,
+            # both passes of the step against the same peak (CUDA events around each pass)
+            "per_kernel": [{"kernel": f"k_{k}{'32' if fp32 else ''}", "algorithmic_bytes_per_launch": b[k],
+                            "ms_per_launch": t_head[f"{k}_ms"],
+                            "achieved": b[k] / (t_head[f"{k}_ms"] / 1e3) / 1e9,
+                            "frac": b[k] / (t_head[f"{k}_ms"] / 1e3) / 1e9 / peak}
+                           for k in ("link", "voxel") if t_head[f"{k}_ms"] > 0]}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
