@@ -82,6 +82,15 @@ VX_HD f3 to_rotation_vector(const q4& q) {
   // |v| = sin(angle/2) comes from the vector part: no cancellation for w close to 1.
   float sl = q.x * q.x + q.y * q.y + q.z * q.z;
   if (sl <= 0.0f) return F3(0, 0, 0);
+  if (q.w > 0.0f) {
+    // small rotations (all but a few links): with r = |v| / w, angle / |v| = 2 atan(r) / (r w)
+    // = (2 / w)(1 - r^2/3 + r^4/5 - ...); for r^2 < 1e-4 the next term is below 2e-13
+    const float iw = 1.0f / q.w, r2 = sl * iw * iw;
+    if (r2 < 1e-4f) {
+      const float k = 2.0f * iw * (1.0f - r2 * (1.0f / 3.0f) + r2 * r2 * 0.2f);
+      return F3(k * q.x, k * q.y, k * q.z);
+    }
+  }
   float vl = sqrtf(sl);
   float ang = 2.0f * atan2f(vl, q.w);  // same angle as 2 acos(w) on a unit quaternion
   float k = ang / vl;
