@@ -406,6 +406,10 @@ def run_ours(args, world, rank, local):
         what = "the full scene" if W.sample_desc is None else f"{W.sample_desc}, {cs.n_voxels} voxels"
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{n} doTimeStep calls of {what} in {el:.1f} s (OpenMP, C-library math)"}
+        # the serial build beside it (the reference's default build has no OpenMP)
+        srate, sn, sel = cpu_oracle_rate(cs, 1, max(2.0, args.cpu_seconds / 3), actuation=W.actuation)
+        cpu["serial"] = {"value": srate, "unit": UNIT, "cores": 1,
+                         "sample": f"{sn} doTimeStep calls of {what} in {sel:.1f} s (one thread)"}
 
     o = t_other
     line = {"metric": W.metric, "value": t_head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
