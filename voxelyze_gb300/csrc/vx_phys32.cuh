@@ -319,7 +319,8 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
   q4 angle1 = Q4(1, 0, 0, 0);
   float px = s + ex;
   float smallTurn = (fabsf(pz) + fabsf(py)) / px;
-  float extendPerc = fabsf((ex - rd) / L);
+  const float iL = 1.0f / L;  // one division for the two uses of the current length
+  float extendPerc = fabsf((ex - rd) * iL);
   const float HF = 1.2f, BEND = 0.05f, EXT = 0.50f;
   if (!smallAngle && smallTurn < BEND && extendPerc < EXT) {
     smallAngle = true;
@@ -356,7 +357,7 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
     B.tArea[l] = tArea;
     B.tSS[l] = tSS;
   }
-  float axial = pos2.x / L;
+  float axial = pos2.x * iL;
   float maxStrain = in.maxStrain, strainOffset = in.strainOffset, stress;
   if (m.linear) {
     if (axial > maxStrain) maxStrain = axial;
@@ -388,7 +389,8 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
     mP = F3(a2c * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z));
     if (lvv) {
       f3 pc = F3(m.sqA1 * dPos2.x, m.sqB1 * dPos2.y - m.sqB2xFMp * (dA1.z + dA2.z), m.sqB1 * dPos2.z + m.sqB2xFMp * (dA1.y + dA2.y));
-      float dmN = 2 * mn.sqrtMass * mn.zetaInternal / pdt, dmP = 2 * mp.sqrtMass * mp.zetaInternal / pdt;
+      const float ipdt = 1.0f / pdt;
+      float dmN = 2 * mn.sqrtMass * mn.zetaInternal * ipdt, dmP = 2 * mp.sqrtMass * mp.zetaInternal * ipdt;
       fN.x += dmN * pc.x; fN.y += dmN * pc.y; fN.z += dmN * pc.z;
       fP.x -= dmP * pc.x; fP.y -= dmP * pc.y; fP.z -= dmP * pc.z;
       float hN = 0.5f * dmN, hP = 0.5f * dmP;
