@@ -63,6 +63,20 @@ def test_cantilever_full_horizon(product_lib, cr_oracle):
     _run_exact(g, o, 10000, 2500, dt)
 
 
+def test_large_angle_branch(product_lib, cr_oracle):
+    """20 voxels in a row, E = 10 kPa, a small tip load: links cross into and out of the
+    large-angle branch all through 2,000 steps (acos/sin/cos, src/VX_Link.cpp:92-110)."""
+    g, o = _pair(product_lib, cr_oracle, S.cantilever(20, 1, 1, E=1e4, tip_force=-0.02))
+    dt = o.recommended_time_step()
+    assert g.recommended_time_step() == dt
+    large = 0
+    for n in (250, 250, 250, 250, 1000):
+        assert g.do_time_steps(n, dt) == o.do_time_steps(n, dt) == n
+        assert state_diff(g, o) == []
+        large += int((g.link_state()["smallAngle"] == 0).sum())
+    assert large > 0
+
+
 def test_single_steps_equal_batched(product_lib, cr_oracle):
     sc = S.cantilever(10, 3, 2, voxel_size=0.005, tip_force=-0.02)
     a = make_sim(product_lib, "vx", sc)

@@ -64,6 +64,9 @@ SCENES_LIVE = [
     ("lattice_dt_every_step", lambda: S.lattice(8, 8, 6, seed=5), [20, 20], "every"),
     ("porous_collisions", lambda: S.porous(14, sigma=1.2), [100, 150], "fixed"),
     ("population", lambda: S.population(6, 3, 6), [100], "fixed"),
+    # 20 voxels in a row, E = 10 kPa: links cross into and out of the large-angle branch
+    # (CVX_Link::orientLink, src/VX_Link.cpp:92-110: acos/sin/cos of the C library)
+    ("floppy_large_angle", lambda: S.cantilever(20, 1, 1, E=1e4, tip_force=-0.02), [250, 250, 250, 250, 1000], "fixed"),
 ]
 
 
@@ -77,12 +80,16 @@ def test_oracle_matches_live_reference(oracle_lib, ref_lib, name, mk, chunks, mo
     dt = a.recommended_time_step()
     assert dt == b.recommended_time_step()
     use = -1.0 if mode == "every" else dt
+    large = 0
     for n in chunks:
         assert a.do_time_steps(n, use) == b.do_time_steps(n, use)
         assert state_diff(a, b) == []
         if sc.collisions:
             assert np.array_equal(a.collisions(), b.collisions())
+        large += int((b.link_state()["smallAngle"] == 0).sum())
     assert a.current_time() == b.current_time()
+    if name == "floppy_large_angle":
+        assert large > 0
 
 
 def _custom(s):
