@@ -118,6 +118,17 @@ def test_decision_replay_follows_the_recorded_branches(product_lib):
     assert not np.array_equal(own, dec)
 
 
+def test_adjoint_refuses_while_decisions_are_recorded(product_lib):
+    sc = S.graded_population(2, 4, 0.7, seed=3)
+    g, eng = G.build(product_lib, sc, sc.phase, AMP, FREQ)
+    dt = g.recommended_time_step()
+    eng.set_decisions(1, 5)
+    with pytest.raises(RuntimeError, match="decisions"):
+        eng.adjoint_com_x(10, dt, G.body_offsets(sc), checkpoint_every=5)
+    eng.set_decisions(0)
+    eng.adjoint_com_x(10, dt, G.body_offsets(sc), checkpoint_every=5)
+
+
 def test_adjoint_rejects_out_of_scope(product_lib):
     sc = S.graded_population(2, 4, 0.7, seed=3)
     sc.materials[0].nu = 0.3

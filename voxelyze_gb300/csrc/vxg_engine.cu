@@ -1699,6 +1699,9 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
     return VXG_E_ARG;
   if (!e->have_globals) return fail(e, VXG_E_STATE, "vxg_set_globals was not called");
   if (e->precision != VXG_FP64) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: the FP64 precision is differentiated");
+  // its steps do not go through vxg_step, which bounds the decision rows
+  if (e->dec_mode)
+    return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: branch decisions are being recorded or replayed (mode 0 first)");
   if (e->adj_scope) return fail(e, VXG_E_STATE, e->adj_scope);
   if (e->g.collisions) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: collisions are outside the differentiated scope");
   if (e->g.any_poisson) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: Poisson's ratio must be 0");
