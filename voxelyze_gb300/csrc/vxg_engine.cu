@@ -1125,6 +1125,11 @@ int vxg_resize(vxg_engine* e, int nv, int nl) {
   VXG_CK(cudaSetDevice(e->device));
   VXG_CK(cudaStreamSynchronize(e->stream));
   release_arena(e);
+  // decision rows are sized by the voxel count: a new scene starts without them
+  if (e->d_dec) cudaFree(e->d_dec);
+  e->d_dec = nullptr;
+  e->dec_cap = e->dec_step = 0;
+  e->dec_mode = 0;
   e->nv = nv;
   e->nl = nl;
   size_t off[VXG_F_COUNT] = {};
@@ -1925,7 +1930,9 @@ int vxg_set_actuation(vxg_engine* e, int mode, double amplitude, double frequenc
 
 int vxg_body_com(vxg_engine* e, const int* offsets, int n_bodies, double* out) {
   if (!e || !offsets || !out || n_bodies <= 0) return VXG_E_ARG;
-  if (offsets[0] < 0 || offsets[n_bodies] > e->nv) return fail(e, VXG_E_SIZE, "vxg_body_com: offsets out of range");
+  for (int b = 0; b < n_bodies; ++b)  // each body a range inside the scene
+    if (offsets[b] < 0 || offsets[b + 1] < offsets[b] || offsets[b + 1] > e->nv)
+      return fail(e, VXG_E_SIZE, "vxg_body_com: offsets out of range");
   VXG_CK(cudaSetDevice(e->device));
   if (int rc = check_topology(e)) return rc;
   if (n_bodies > e->n_body_cap) {
