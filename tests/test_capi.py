@@ -37,3 +37,12 @@ def test_product_does_not_link_the_oracle(product_lib):
     deps = open("/proc/self/maps").read()
     assert "libvxoracle" not in os.path.basename(path)
     assert os.path.exists(path) and deps  # loaded in-tree
+
+
+def test_python_binding_uses_declared_entry_points(product_lib):
+    """Every vx_* function voxelyze_gb300.facade binds is declared in include/vx_capi.h."""
+    from voxelyze_gb300 import facade as F
+
+    declared = set(_declared("vx_capi.h"))
+    bound = {f"vx_{k}" for d in (F._SIGS, F._OPT_SIGS, F._EXT_SIGS) for k in d}
+    assert sorted(bound - declared) == []
