@@ -76,8 +76,9 @@ float vx_state_info_device(void* s, int info, int type);    /* GPU reduction, se
  * leaves it at zero.  The first call on a device looks the scratch up and may make the CUDA runtime
  * load this library's device code: make it before any stream capture.  Calls that overlap in time
  * on one device (several threads, streams or simulations) share the scratch and race: serialise
- * them.  Host edits not yet on the device are refused (VXG_E_STATE), not uploaded.  Returns 0, or
- * a VXG_E_* code with a static message in *why (why may be NULL). */
+ * them.  Host edits not yet on the device are refused (VXG_E_STATE), not uploaded, and so is a
+ * scene whose indices no step has checked yet.  Returns 0, or a VXG_E_* code with a static
+ * message in *why (why may be NULL). */
 int vx_state_info_into(void* s, int info, int type, float* d_out, const char** why);
 int vx_counters(void* s, long long* out, int n);            /* vxg_counters of the engine */
 int vx_enable_timing(void* s, int on);                      /* vxg_enable_timing */
