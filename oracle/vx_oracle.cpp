@@ -5,7 +5,7 @@
 // bench.py's CPU-baseline leg.  It exposes the vxo_* facade (oracle/facade.h).
 //
 // Parity pin: its results are compared bit for bit with the reference library compiled from its own
-// sources (oracle/_ref, tests/test_oracle_vs_reference.py) and with committed golden vectors
+// sources (oracle/_ref, tests/test_oracle_reference.py) and with committed golden vectors
 // generated from that build (tests/golden/, tests/golden/make_golden.py).
 //
 // Every routine cites the reference file:line it restates.  Float/double promotions follow the
