@@ -167,3 +167,79 @@ def test_cpp_scene_file_calls(product_lib, tmp_path):
                          capture_output=True, text=True).stdout.split()
     got = dict(zip(out[::2], out[1::2]))
     assert got == {"voxels": "3", "links": "2", "materials": "1", "nu": "0.3", "loaded": "1", "same": "1"}
+
+
+def _random_scene(lib, prefix, seed):
+    """Seeded random scene: 1-4 linear materials with random E, density, Poisson's ratio, CTE,
+    friction and damping; a random occupancy of a small box with a random material per voxel;
+    random externals (fixed DOFs, prescribed translations and rotations, forces, moments)."""
+    rng = np.random.default_rng(seed)
+    sim = F.Sim(lib, prefix, float(rng.choice([0.001, 0.005, 0.01])))
+    mats = []
+    for _ in range(int(rng.integers(1, 5))):
+        E, rho = float(10 ** rng.uniform(4, 7)), float(rng.uniform(500, 3000))
+        m = sim.add_material(E, rho)
+        if rng.random() < 0.5:
+            sim.material_set(m, F.PROP_POISSON, float(rng.uniform(0, 0.45)))
+        sim.material_set(m, F.PROP_CTE, float(rng.uniform(0, 0.02)))
+        sim.material_set(m, F.PROP_MU_STATIC, float(rng.uniform(0, 1)))
+        sim.material_set(m, F.PROP_MU_KINETIC, float(rng.uniform(0, 0.5)))
+        sim.material_set(m, F.PROP_ZETA_GLOBAL, float(rng.uniform(0, 0.2)))
+        if rng.random() < 0.3:
+            sim.set_model_linear(m, E, float(rng.uniform(0.05, 0.5)))
+        mats.append(m)
+    n = 0
+    for z in range(3):
+        for y in range(4):
+            for x in range(5):
+                if rng.random() < 0.6:
+                    sim.set_voxel(mats[int(rng.integers(len(mats)))], x, y, z)
+                    n += 1
+    for v in rng.choice(n, size=min(n, 6), replace=False) if n else []:
+        v = int(v)
+        kind = int(rng.integers(4))
+        if kind == 0:
+            sim.set_fixed(v, int(rng.integers(1, 64)))
+        elif kind == 1:
+            sim.set_force(v, *(float(x) for x in rng.normal(0, 1, 3)))
+        elif kind == 2:
+            sim.set_moment(v, *(float(x) for x in rng.normal(0, 1e-3, 3)))
+        else:
+            sim.set_displacement(v, int(rng.choice([F.X_TRANSLATE, F.Y_TRANSLATE, F.Z_TRANSLATE])),
+                                 float(rng.normal(0, 1e-3)))
+    return sim
+
+
+def _within_one_ulp(a, b):
+    """Equal JSON values, numbers allowed to differ by one ulp."""
+    if isinstance(a, dict):
+        return isinstance(b, dict) and a.keys() == b.keys() and all(_within_one_ulp(a[k], b[k]) for k in a)
+    if isinstance(a, list):
+        return isinstance(b, list) and len(a) == len(b) and all(_within_one_ulp(x, y) for x, y in zip(a, b))
+    if isinstance(a, float) and isinstance(b, float):
+        return a == b or np.nextafter(a, b) == b
+    return a == b
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_scenes_match_reference_build(product_lib, ref_lib, tmp_path, seed):
+    """Seeded random scenes save to the reference build's document (layout, and every number as a
+    double), and each library loads the other's file back to the same scene.  This library reads
+    every number correctly rounded; the reference's reader (rapidjson's default number parsing)
+    reads some 17-digit numbers one ulp off, so in that direction numbers may differ by one ulp."""
+    ours = save(_random_scene(product_lib, "vx", seed), tmp_path / "p.vxl.json")
+    ref = save(_random_scene(ref_lib, "vxr", seed), tmp_path / "r.vxl.json")
+    lo, no = split(ours)
+    lr, nr = split(ref)
+    assert lo == lr
+    assert no == nr
+    p2 = F.Sim(product_lib, "vx", 0.001)
+    r2 = F.Sim(ref_lib, "vxr", 0.001)
+    assert p2.load_json(str(tmp_path / "r.vxl.json")) and r2.load_json(str(tmp_path / "p.vxl.json"))
+    da = json.loads(save(p2, tmp_path / "p2.vxl.json"))  # ours reading the reference's file
+    db = json.loads(save(r2, tmp_path / "r2.vxl.json"))  # the reference reading ours
+    orig = json.loads(ours)
+    for key in ("voxelSize", "materials", "voxels", "externals"):
+        assert da[key] == orig[key], key                  # exact
+        assert _within_one_ulp(db[key], orig[key]), key
+    assert p2.voxel_count() == r2.voxel_count() and p2.link_count() == r2.link_count()
