@@ -19,6 +19,8 @@ int vx_material_set_model_linear(void* s, int mat, float E, float fail_stress); 
 int vx_material_set_model_bilinear(void* s, int mat, float E, float plastic_E, float yield_stress,
                                    float fail_stress);                            /* src/VX_Material.cpp:389-434 */
 int vx_material_set_model(void* s, int mat, int n, const float* strain, const float* stress); /* :283-350 */
+float vx_material_stress(void* s, int mat, float strain, float tss, int force_linear); /* CVX_Material::stress :165-195 */
+float vx_material_modulus(void* s, int mat, float strain);                            /* CVX_Material::modulus :214-226 */
 int vx_set_voxel(void* s, int mat, int x, int y, int z);    /* setVoxel                 src/Voxelyze.cpp:422-437 */
 int vx_remove_voxel(void* s, int x, int y, int z);          /* setVoxel(NULL, ...)      src/Voxelyze.cpp:424-427, 464-483 */
 int vx_replace_material(void* s, int a, int b);             /* replaceMaterial          src/Voxelyze.cpp:406-420 */

@@ -25,6 +25,8 @@ extern "C" {
   int P##_material_set_model_bilinear(void* s, int mat, float E, float plastic_E, float yield_stress, \
                                       float fail_stress);                                           \
   int P##_material_set_model(void* s, int mat, int n, const float* strain, const float* stress);    \
+  float P##_material_stress(void* s, int mat, float strain, float tss, int force_linear);           \
+  float P##_material_modulus(void* s, int mat, float strain);                                       \
   int P##_set_voxel(void* s, int mat, int x, int y, int z);                                         \
   int P##_set_voxels(void* s, int n, const int* mat, const int* xyz);                               \
   int P##_remove_voxel(void* s, int x, int y, int z);                                               \

@@ -93,6 +93,15 @@ int vxr_material_set_model(void* s, int mat, int n, const float* strain, const f
   return r->mats[mat]->setModel(n, a.data(), b.data()) ? 0 : -1;
 }
 
+float vxr_material_stress(void* s, int mat, float strain, float tss, int force_linear) {
+  RefSim* r = S(s);
+  return r->mats[mat]->stress(strain, tss, force_linear != 0);
+}
+float vxr_material_modulus(void* s, int mat, float strain) {
+  RefSim* r = S(s);
+  return r->mats[mat]->modulus(strain);
+}
+
 int vxr_set_voxel(void* s, int mat, int x, int y, int z) {
   RefSim* r = S(s);
   CVX_Material* m = (mat >= 0 && mat < (int)r->mats.size()) ? r->mats[mat] : nullptr;

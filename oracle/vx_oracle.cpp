@@ -1401,6 +1401,11 @@ int vxo_material_set_model(void* s, int mat, int n, const float* strain, const f
   return ok ? 0 : -1;
 }
 
+float vxo_material_stress(void* s, int mat, float strain, float tss, int force_linear) {
+  return S(s)->vmats[mat].stress(strain, tss, force_linear != 0);
+}
+float vxo_material_modulus(void* s, int mat, float strain) { return S(s)->vmats[mat].modulus(strain); }
+
 int vxo_set_voxel(void* s, int mat, int x, int y, int z) {
   Sim* r = S(s);
   if (mat < 0 || mat >= (int)r->vmats.size()) return -1;

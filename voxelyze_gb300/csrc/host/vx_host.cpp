@@ -1229,6 +1229,16 @@ int vx_material_set_model(void* s, int mat, int n, const float* strain, const fl
   std::vector<float> a(strain, strain + n), b(stress, stress + n);
   return h->mats[mat]->setModel(n, a.data(), b.data()) ? 0 : -1;
 }
+float vx_material_stress(void* s, int mat, float strain, float tss, int force_linear) {
+  Handle* h = H(s);
+  if (mat < 0 || mat >= (int)h->mats.size()) return 0.0f;
+  return h->mats[mat]->stress(strain, tss, force_linear != 0);
+}
+float vx_material_modulus(void* s, int mat, float strain) {
+  Handle* h = H(s);
+  if (mat < 0 || mat >= (int)h->mats.size()) return 0.0f;
+  return h->mats[mat]->modulus(strain);
+}
 int vx_set_voxel(void* s, int mat, int x, int y, int z) {
   Handle* h = H(s);
   CVX_Material* m = (mat >= 0 && mat < (int)h->mats.size()) ? h->mats[mat] : nullptr;

@@ -79,6 +79,8 @@ _SIGS = {
 
 # scene-file entry points: in the product and the reference build, not in the oracle
 _OPT_SIGS = {
+    "material_stress": (_f, [_p, _i, _f, _f, _i]),
+    "material_modulus": (_f, [_p, _i, _f]),
     "load_json": (_i, [_p, C.c_char_p]),
     "save_json": (_i, [_p, C.c_char_p]),
     "mesh_generate": (_i, [_p]),
@@ -152,6 +154,14 @@ class Sim:
         a = np.ascontiguousarray(strain, dtype=np.float32)
         b = np.ascontiguousarray(stress, dtype=np.float32)
         return self.f["material_set_model"](self.h, mat, len(a), _ptr(a, C.c_float), _ptr(b, C.c_float)) == 0
+
+    def material_stress(self, mat, strain, tss=0.0, force_linear=False) -> float:
+        """CVX_Material::stress (src/VX_Material.cpp:165-195)."""
+        return self.f["material_stress"](self.h, mat, strain, tss, 1 if force_linear else 0)
+
+    def material_modulus(self, mat, strain) -> float:
+        """CVX_Material::modulus (src/VX_Material.cpp:214-226)."""
+        return self.f["material_modulus"](self.h, mat, strain)
 
     # -- voxels ----------------------------------------------------------------------------
     def set_voxel(self, mat: int, x: int, y: int, z: int) -> int:
