@@ -79,8 +79,11 @@ float vx_state_info_device(void* s, int info, int type);    /* GPU reduction, se
  * load this library's device code: make it before any stream capture.  Calls that overlap in time
  * on one device (several threads, streams or simulations) share the scratch and race: serialise
  * them.  Host edits not yet on the device are refused (VXG_E_STATE), not uploaded, and so is a
- * scene whose indices no step has checked yet.  Returns 0, or a VXG_E_* code with a static
- * message in *why (why may be NULL). */
+ * scene whose indices no step has checked yet.  In FP32C only the state fields the quantity reads
+ * are converted to FP64 first (none for MASS, ENG_STRESS, ENG_STRAIN).  The simulation's device is
+ * current during the call; the caller's current device is restored before it returns.  Returns 0,
+ * or a VXG_E_* code with a static message in *why (why may be NULL); nothing is written to d_out
+ * then. */
 int vx_state_info_into(void* s, int info, int type, float* d_out, const char** why);
 int vx_counters(void* s, long long* out, int n);            /* vxg_counters of the engine */
 int vx_enable_timing(void* s, int on);                      /* vxg_enable_timing */

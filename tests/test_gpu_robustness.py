@@ -112,3 +112,40 @@ def test_repeat_runs_are_bit_identical(product_lib, precision):
         runs.append(s)
     assert state_diff(*runs) == []
     assert np.array_equal(runs[0].collisions(), runs[1].collisions())
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_shrunk_externals_table_rechecks_indices(product_lib, precision):
+    """A table re-uploaded with fewer entries (here the externals, emptied through the engine ABI)
+    keeps its allocation but not its old count: a voxel still naming an external that is gone makes
+    the next step an index error instead of a read of the stale entry."""
+    sim = make_sim(product_lib, "vx", S.cantilever(6, 2, 2, voxel_size=0.005, tip_force=-0.01))
+    F.Engine(sim).set_precision(precision)
+    assert sim.do_time_steps(5, -1.0) == 5
+    e = _engine(product_lib, sim)
+    product_lib.vxg_set_externals.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    assert product_lib.vxg_set_externals(e, None, 0) == 0
+    assert sim.do_time_steps(5, -1.0) < 0
+    msg = product_lib.vxg_last_error(e).decode()
+    assert "index out of range" in msg and "voxel external" in msg, msg
+
+
+def test_state_info_extremes_start_like_the_reference(product_lib):
+    """stateInfo starts MIN at FLT_MAX and MAX at -FLT_MAX (src/Voxelyze.cpp:755-756): with every
+    voxel's momentum infinite, VELOCITY MIN stays FLT_MAX and MAX is infinite, on the device as on
+    the host."""
+    sim = make_sim(product_lib, "vx", S.lattice(6, 5, 4))
+    assert sim.do_time_steps(2, sim.recommended_time_step()) == 2
+    e = _engine(product_lib, sim)
+    nv = sim.voxel_count()
+    VXG_F_LINMOM = 5
+    mom = np.full(3 * nv, np.inf)
+    assert product_lib.vxg_set_field(e, VXG_F_LINMOM, mom.ctypes.data, 3 * nv) == 0
+    dev = product_lib.vx_state_info_device
+    dev.restype = C.c_float
+    dev.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    flt_max = float(np.finfo(np.float32).max)
+    assert dev(C.c_void_p(sim.h), F.VELOCITY, F.MIN) == flt_max
+    assert dev(C.c_void_p(sim.h), F.VELOCITY, F.MAX) == np.inf
+    assert sim.state_info(F.VELOCITY, F.MIN) == flt_max
+    assert sim.state_info(F.VELOCITY, F.MAX) == np.inf
