@@ -166,9 +166,10 @@ class Workload:
     """One seeded synthetic scene of the benchmark set; ``scene()`` builds the full case and
     ``cpu_sample()`` the bounded sample the CPU baseline steps (the full scene unless stated)."""
 
-    def __init__(self, name, metric, desc, scene, cpu_sample=None, actuation=None, sample_desc=None):
+    def __init__(self, name, metric, desc, scene, cpu_sample=None, actuation=None, sample_desc=None, horizon=1000):
         self.name, self.metric, self.desc = name, metric, desc
         self.scene = scene
+        self.horizon = horizon                # steps over which the FP32C error is reported
         self.cpu_sample = cpu_sample or scene
         self.actuation = actuation            # (amplitude, frequency) of in-step CTE actuation
         self.sample_desc = sample_desc
@@ -185,11 +186,12 @@ def workloads():
             lambda: S.lattice(*DIMS)),
         "cantilever": Workload(
             "cantilever", "voxel-steps/s (40x8x8 cantilever)",
-            "cantilever 40x8x8, 5 mm, E 1 MPa, x=0 face fixed, -1 N per tip voxel", lambda: S.cantilever(40, 8, 8)),
+            "cantilever 40x8x8, 5 mm, E 1 MPa, x=0 face fixed, -1 N per tip voxel", lambda: S.cantilever(40, 8, 8),
+            horizon=10000),
         "porous": Workload(
             "porous", "voxel-steps/s (64^3 porous body, collisions)",
             "porous 64^3 (sigma 3, void 0.4), nu 0.35, dropped 2 voxels onto the floor, gravity, collisions, "
-            "friction 1.0/0.5", lambda: S.porous(64)),
+            "friction 1.0/0.5", lambda: S.porous(64), horizon=5000),
         "population": Workload(
             "population", "voxel-steps/s (4,096 independent bodies)",
             "4,096 bodies, sides 4..24, occupancy 0.6, passive/active CTE materials, floor+gravity, friction "
@@ -327,11 +329,19 @@ def run_ours(args, world, rank, local):
         t["value"], _, secs = aggregate_rate(nv * args.steps, t["total_ms"] / 1e3)
         t["total_ms"] = 1e3 * secs
 
-    # FP32C error against the FP64 path (bit-identical to the FP64 oracle) after the same steps
+    # FP32C error against the FP64 path (bit-identical to the FP64 oracle), both run on to the
+    # workload's horizon (1,000 steps for the lattice; the population stops at 1,000 of its 10,000)
+    done = args.warmup + 2 * args.steps
+    if not args.quick_error:
+        more = max(0, W.horizon - done)
+        for sim in (sim64, sim32):
+            if more and sim.do_time_steps(more, dt) != more:
+                raise RuntimeError("diverged on the way to the error horizon")
+        done += more
     p64 = sim64.voxel_state()["pos"]
     p32 = sim32.voxel_state()["pos"]
     disp = p64 - sc.xyz * sc.voxel_size
-    err = {"steps": args.warmup + 2 * args.steps,
+    err = {"steps": done,
            "rel_pos": float(np.abs(p32 - p64).max() / np.abs(p64).max()),
            "rel_disp": float(np.abs(p32 - p64).max() / max(np.abs(disp).max(), 1e-30))}
     extra = {}
@@ -398,6 +408,29 @@ def run_ours(args, world, rank, local):
                             "frac": b[k] / (t_head[f"{k}_ms"] / 1e3) / 1e9 / peak}
                            for k in ("link", "voxel") if t_head[f"{k}_ms"] > 0]}
 
+    # FP64 path against the FP64 pipe: its link pass issues double operations, not bytes, at the
+    # rate that bounds it.  Instructions per link counted by ncu on the same generator (roofline.py),
+    # peak measured here by vxg_probe_fp64_rate.
+    o64 = t_other if fp32 else t_head
+    fp64_roof = None
+    fma_s, probe_ms = C.c_double(0), C.c_float(0)
+    lib.vxg_probe_fp64_rate.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_float)]
+    if lib.vxg_probe_fp64_rate(0, 4096, C.byref(fma_s), C.byref(probe_ms)) == 0 and fma_s.value > 0:
+        f = R.fp64_ops(nv, nl, poisson=poisson)
+        if f is not None and o64["link_ms"] > 0:
+            ach = f["link_flops"] / (o64["link_ms"] / 1e3) / 1e9
+            ach_i = f["link_pipe_inst"] / (o64["link_ms"] / 1e3) / 1e9
+            peak_flops = 2 * fma_s.value / 1e9
+            peak_inst = fma_s.value / 32 / 1e9  # warp instructions
+            fp64_roof = {"bound": "fp64", "kernel": "k_link (FP64 link pass)", "achieved": ach, "peak": peak_flops,
+                         "unit": "GFLOP/s", "frac": ach / peak_flops,
+                         "pipe_inst_per_s": {"achieved": 1e9 * ach_i, "peak": 1e9 * peak_inst,
+                                             "frac": ach_i / peak_inst},
+                         "flops_per_launch": f["link_flops"], "ms_per_launch": o64["link_ms"],
+                         "peak_source": "measured: vxg_probe_fp64_rate (fma.rn.f64 chains on every SM, "
+                                        "%.3f ms best of 5)" % probe_ms.value,
+                         "counts": "ncu instruction counts per link, roofline.FP64_OPS"}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
@@ -428,7 +461,7 @@ def run_ours(args, world, rank, local):
                                                            "voxel": o["voxel_ms"]}},
                        "fp32c_over_fp64": (t_head["value"] / o["value"]) if fp32 else (o["value"] / t_head["value"]),
                        "fp32c_error_vs_fp64": err, **extra},
-            "roofline": roof, "cpu_baseline": cpu,
+            "roofline": roof, "roofline_fp64": fp64_roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * nv, "d2h_bytes_per_step": 24 * nv,
                     "steps": e2e_steps},
             "clocks": t_head["clocks"], "gpu_launches": t_head["launches"]}
@@ -513,6 +546,8 @@ def main():
     ap.add_argument("--precision", default="fp32c", choices=["fp64", "fp32c"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick-error", action="store_true",
+                    help="report the FP32C error where the timed steps end, not at the workload's horizon")
     ap.add_argument("--dims", default="128,128,64", help="lattice size (smaller cases for profiling)")
     ap.add_argument("--workload", default="lattice",
                     choices=["lattice", "cantilever", "porous", "population", "adjoint"],

@@ -216,6 +216,13 @@ int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_
  * Both give identical results. */
 int vxg_set_link_pipeline(vxg_engine* e, int blocks_per_sm);
 int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm);
+/* FP32C link pass at a fixed dt, one thread per link: on (1, the default) a small-angle kernel runs
+ * every link that stays in CVX_Link::orientLink's small-angle branch (src/VX_Link.cpp:92-110) and a
+ * general kernel the links it deferred (large-angle, or leaving the branch this step); off (0) the
+ * general kernel runs every link.  Results are bit-identical either way.  vxg_autotune compares
+ * both. */
+int vxg_set_link_split(vxg_engine* e, int on);
+int vxg_get_link_split(vxg_engine* e, int* on);
 /* Branch decisions of the FP64 voxel pass (no counterpart in the reference), for finite differences
  * that follow one run's branches: mode 1 records, for each of the next `steps` steps, every voxel's
  * floor-contact and static-friction decisions (CVX_Voxel::floorForce and the static-friction latch
@@ -266,6 +273,10 @@ int vxg_last_batch_ms(vxg_engine* e, float* ms);
 const char* vxg_last_error(const vxg_engine* e);
 void* vxg_stream(vxg_engine* e); /* cudaStream_t the engine launches on */
 int vxg_synchronize(vxg_engine* e);
+/* FP64 fused multiply-adds per second that `device` sustains (independent fma.rn.f64 chains on
+ * every SM, best of five event-timed launches of `iters` iterations): the measured denominator of
+ * the FP64 path's compute roofline.  No counterpart in the reference.  *ms = the best launch. */
+int vxg_probe_fp64_rate(int device, int iters, double* fma_per_s, float* ms);
 
 #ifdef __cplusplus
 }

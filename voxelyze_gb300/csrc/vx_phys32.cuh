@@ -48,6 +48,7 @@ struct View {
   float* mN;
   float* mP;
   float* restDelta; // nl: rest length - nominal size
+  int* large;       // nl: links the small-angle link pass deferred to the general one this step
   float s;          // nominal voxel size
 };
 
@@ -292,12 +293,18 @@ VX_HD LinkIn link_gather(const View& S, int l) {
 // CVX_Link::updateForces + orientLink + updateStrain in FP32C for link l from its gathered inputs;
 // writes the link's new state and returns the axial strain (the divergence test's value).
 // pdt is every voxel's previous time step (the local damping divides by it).
-VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
+// SMALL: the caller has seen the small-angle flag set.  The link's angle1 is then the identity and
+// its rotation vector zero for the whole step, unless the hysteresis test below moves it to the
+// large-angle branch: in that case nothing is written, *deferred is set, and the general form
+// (SMALL = false) must process the link from the same inputs.  For a link that stays small-angle
+// both forms evaluate the same expressions in the same order, so their results are bit-identical.
+template <bool SMALL>
+VX_HDN float link_compute_t(const View& S, int l, const LinkIn& in, float pdt, bool* deferred) {
   const vx64::View& B = S.B;
   const int nl = B.nl;
   uint32_t lf = in.lf;
   int axis = (lf >> 8) & 3;
-  bool smallAngle = lf & VXG_LF_SMALL_ANGLE;
+  bool smallAngle = SMALL || (lf & VXG_LF_SMALL_ANGLE);
   bool lvv = lf & VXG_LF_LOCAL_VEL_VALID;
   const vxg_link_material& m = B.lm[in.lmat];
   const float s = S.s;
@@ -322,7 +329,12 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
   const float iL = 1.0f / L;  // one division for the two uses of the current length
   float extendPerc = fabsf((ex - rd) * iL);
   const float HF = 1.2f, BEND = 0.05f, EXT = 0.50f;
-  if (!smallAngle && smallTurn < BEND && extendPerc < EXT) {
+  if (SMALL) {
+    if (smallTurn > HF * BEND || extendPerc > HF * EXT) {
+      *deferred = true;
+      return 0.0f;
+    }
+  } else if (!smallAngle && smallTurn < BEND && extendPerc < EXT) {
     smallAngle = true;
     lvv = false;
   } else if (smallAngle && (smallTurn > HF * BEND || extendPerc > HF * EXT)) {
@@ -330,7 +342,7 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
     lvv = false;
   }
   f3 pos2;
-  if (smallAngle) {
+  if (SMALL || smallAngle) {
     pos2 = F3(ex - rd, py, pz);
   } else {
     from_angle_to_pos_x(angle1, F3(px, py, pz));
@@ -339,10 +351,10 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
     float lms = (ex * (2.0f * s + ex) + py * py + pz * pz) / (len + s);  // |pos2| - s
     pos2 = F3(lms - rd, 0, 0);
   }
-  f3 a1v = to_rotation_vector(angle1);
+  const f3 a1v = SMALL ? F3(0, 0, 0) : to_rotation_vector(angle1);  // the identity's rotation vector is +0
   f3 a2v = to_rotation_vector(angle2);
   st3(S.pos2, nl, l, pos2);
-  if (!(smallAngle && (lf & VXG_LF_SMALL_ANGLE))) st3(S.a1v, nl, l, a1v);  // else zeros, already stored
+  if (!SMALL && !(smallAngle && (lf & VXG_LF_SMALL_ANGLE))) st3(S.a1v, nl, l, a1v);  // else zeros, already stored
   st3(S.a2v, nl, l, a2v);
   f3 dPos2 = F3(0.5f * (pos2.x - oldPos2.x), 0.5f * (pos2.y - oldPos2.y), 0.5f * (pos2.z - oldPos2.z));
   f3 dA1 = F3(0.5f * (a1v.x - oldA1.x), 0.5f * (a1v.y - oldA1.y), 0.5f * (a1v.z - oldA1.z));
@@ -403,7 +415,7 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
     } else {
       lvv = true;
     }
-    if (!smallAngle) {
+    if (!SMALL && !smallAngle) {
       fN = rotate_inv(angle1, fN);
       mN = rotate_inv(angle1, mN);
     }
@@ -422,10 +434,39 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
   if (nf != lf) B.lflags[l] = nf;
   return axial;
 }
+VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
+  return link_compute_t<false>(S, l, in, pdt, nullptr);
+}
 
 template <bool POIS>
 VX_HDN float link_update(const View& S, int l) {
   return link_compute(S, l, link_gather<POIS>(S, l), S.B.ctl->last_dt);  // every voxel stepped with last_dt
+}
+
+// The small-angle form for link l whose flags lf the caller has read and found small-angle:
+// gathers the rest of the link's inputs (its angle1v is zero and is not read) and computes it.
+// Returns the axial strain, or sets *deferred (nothing written) if the link leaves the branch.
+template <bool POIS>
+VX_HDN float link_update_small(const View& S, int l, uint32_t lf, bool* deferred) {
+  const vx64::View& B = S.B;
+  const int nl = B.nl;
+  LinkIn in;
+  in.lf = lf;
+  in.lmat = B.lmat[l];
+  in.oldPos2 = ld3(S.pos2, nl, l);
+  in.oldA1 = F3(0, 0, 0);
+  in.oldA2 = ld3(S.a2v, nl, l);
+  if (!POIS || B.lm[in.lmat].nu == 0.0f) {
+    in.tArea = B.tArea[l];
+    in.tSS = B.tSS[l];
+  } else {
+    in.tArea = in.tSS = 0.0f;
+  }
+  in.maxStrain = B.maxStrain[l];
+  in.strainOffset = B.strainOffset[l];
+  const int vn = B.lvox[l], vp = B.lvox[nl + l];
+  link_gather_ends<POIS>(S, l, in, vn, vp);
+  return link_compute_t<true>(S, l, in, B.ctl->last_dt, deferred);
 }
 
 

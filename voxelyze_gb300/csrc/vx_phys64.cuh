@@ -55,6 +55,8 @@ struct Ctl {
   int steps;            // completed steps in this batch
   int status;           // device error bits
   unsigned maxf[2];     // recommendedTimeStep maximum (float bits), double-buffered by step parity
+  int n_large;          // FP32C split link pass: links deferred to the general kernel this step
+  int pad_;
   float time;           // CVoxelyze::currentTime
   float last_dt;
   unsigned long long counters[VXG_C_COUNT];

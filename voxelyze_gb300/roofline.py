@@ -85,3 +85,27 @@ def measured_traffic(kind: str, n_voxels: int, n_links: int):
     if t is None:
         return None
     return t["per_voxel"] * n_voxels + t["per_link"] * n_links
+
+
+# FP64 path against the FP64 pipe.  Double-precision instructions per unit counted by ncu
+# (sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum and sm__inst_executed_pipe_fp64.sum,
+# one launch of each pass of the FP64 path after warm-up) on the bench's lattice generator, divided by
+# the units of the launch.  FLOPs count an FMA as two.  None until measured.
+FP64_OPS = {
+    "link": None,   # {"dadd": .., "dmul": .., "dfma": .., "pipe_warp_inst": ..} per link
+    "voxel": None,  # the same per voxel
+}
+
+
+def fp64_ops(n_voxels: int, n_links: int, poisson: bool):
+    """FLOPs and FP64-pipe warp instructions of one FP64 link pass (and voxel pass) at this size, or
+    None if the counts have not been measured."""
+    L, V = FP64_OPS["link"], FP64_OPS["voxel"]
+    if L is None:
+        return None
+    out = {"link_flops": (L["dadd"] + L["dmul"] + 2 * L["dfma"]) * n_links,
+           "link_pipe_inst": L["pipe_warp_inst"] * n_links}
+    if V is not None:
+        out["voxel_flops"] = (V["dadd"] + V["dmul"] + 2 * V["dfma"]) * n_voxels
+        out["voxel_pipe_inst"] = V["pipe_warp_inst"] * n_voxels
+    return out
