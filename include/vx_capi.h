@@ -60,6 +60,23 @@ int vx_get_voxel_state(void* s, double* d13, float* f5, int* i2);
 int vx_get_link_state(void* s, double* d22, float* f6, int* i6);
 int vx_get_collisions(void* s, int* pairs, int cap);        /* collisionList() as index pairs */
 float vx_state_info(void* s, int info, int type);           /* stateInfo                src/Voxelyze.cpp:752-800 */
+/* per-voxel and per-link queries, read from the state after the last step (the first read after a
+ * step downloads it from the GPU).  Voxels by voxel-list index, links by link-list index, corners
+ * as CVX_Voxel::voxelCorner (bit 2 = +x, bit 1 = +y, bit 0 = +z).  A voxel without an external
+ * gives zero external force and moment (the reference dereferences its missing external there).
+ * force/moment leave out collision contact forces, which stay on the GPU. */
+int vx_voxel_external_force(void* s, int v, float* out3);   /* CVX_Voxel::externalForce   src/VX_Voxel.cpp:117-127 */
+int vx_voxel_external_moment(void* s, int v, float* out3);  /* CVX_Voxel::externalMoment  src/VX_Voxel.cpp:129-139 */
+int vx_voxel_corner_offset(void* s, int v, int corner, float* out3);   /* cornerOffset   src/VX_Voxel.cpp:146-159 */
+int vx_voxel_corner_position(void* s, int v, int corner, float* out3); /* cornerPosition src/VX_Voxel.cpp:141-144 */
+int vx_voxel_force(void* s, int v, double* out3);           /* CVX_Voxel::force           src/VX_Voxel.cpp:234-256 */
+int vx_voxel_moment(void* s, int v, double* out3);          /* CVX_Voxel::moment          src/VX_Voxel.cpp:258-271 */
+int vx_voxel_is_yielded(void* s, int v);                    /* CVX_Voxel::isYielded: 1/0  src/VX_Voxel.cpp:92-98 */
+int vx_voxel_is_failed(void* s, int v);                     /* CVX_Voxel::isFailed: 1/0   src/VX_Voxel.cpp:100-106 */
+float vx_voxel_pressure(void* s, int v);                    /* CVX_Voxel::pressure        include/VX_Voxel.h:103-104 */
+float vx_link_strain_energy(void* s, int l);                /* CVX_Link::strainEnergy     src/VX_Link.cpp:251-257 */
+int vx_link_is_yielded(void* s, int l);                     /* CVX_Link::isYielded: 1/0   src/VX_Link.cpp:127-130 */
+int vx_link_is_failed(void* s, int l);                      /* CVX_Link::isFailed: 1/0    src/VX_Link.cpp:132-135 */
 
 /* extensions for throughput users */
 int vx_set_precision(void* s, int mode);                    /* 0 = FP64 (default), 1 = FP32C */
@@ -103,6 +120,8 @@ int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk); /*
 int vx_autotune(void* s, int trial_steps, float dt, int* out3);            /* vxg_autotune: link, voxel, chunk */
 int vx_set_link_pipeline(void* s, int blocks_per_sm);                      /* vxg_set_link_pipeline */
 int vx_get_link_pipeline(void* s, int* blocks_per_sm);                     /* vxg_get_link_pipeline */
+int vx_set_link_split(void* s, int on);                                    /* vxg_set_link_split */
+int vx_get_link_split(void* s, int* on);                                   /* vxg_get_link_split */
 int vx_set_poisson_fusion(void* s, int on);                                /* vxg_set_poisson_fusion */
 /* the engine behind a handle (include/vxg.h), pending host edits uploaded first; NULL on failure.
  * No counterpart in the reference: for callers that mix the engine ABI with this facade. */

@@ -8,8 +8,14 @@
 # Flags follow the reference makefile (-O3 -std=c++11) without -DPARDISO_5 (PARDISO is absent and
 # off the time-step path) and with -ffp-contract=off so no platform contracts a*b+c into an FMA.
 # The shipped lib/libvoxelyze.0.9.a is never used.
+#
+# Usage: build_ref.sh REFERENCE_ROOT   (the checkout holding the reference's include/ and src/)
 set -euo pipefail
-REF=${VOXELYZE_REFERENCE:-/root/reference}
+if [ $# -lt 1 ]; then
+  echo "usage: $0 REFERENCE_ROOT" >&2
+  exit 2
+fi
+REF=$1
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src" ]; then

@@ -56,7 +56,19 @@ extern "C" {
   int P##_get_voxel_state(void* s, double* d13, float* f5, int* i2);                                \
   int P##_get_link_state(void* s, double* d22, float* f6, int* i6);                                 \
   int P##_get_collisions(void* s, int* pairs, int cap);                                             \
-  float P##_state_info(void* s, int info, int type);
+  float P##_state_info(void* s, int info, int type);                                               \
+  int P##_voxel_external_force(void* s, int v, float* out3);                                        \
+  int P##_voxel_external_moment(void* s, int v, float* out3);                                       \
+  int P##_voxel_corner_offset(void* s, int v, int corner, float* out3);                             \
+  int P##_voxel_corner_position(void* s, int v, int corner, float* out3);                           \
+  int P##_voxel_force(void* s, int v, double* out3);                                                \
+  int P##_voxel_moment(void* s, int v, double* out3);                                               \
+  int P##_voxel_is_yielded(void* s, int v);                                                         \
+  int P##_voxel_is_failed(void* s, int v);                                                          \
+  float P##_voxel_pressure(void* s, int v);                                                         \
+  float P##_link_strain_energy(void* s, int l);                                                     \
+  int P##_link_is_yielded(void* s, int l);                                                          \
+  int P##_link_is_failed(void* s, int l);
 
 /* material property ids for *_material_set (VX_Material.h:75-107) */
 enum {

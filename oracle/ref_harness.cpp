@@ -328,6 +328,60 @@ int vxr_get_collisions(void* s, int* pairs, int cap) {
   return n;
 }
 
+// per-voxel and per-link queries through the reference's own methods (VX_Voxel.h:79-130,
+// VX_Link.h:47-66).  externalForce/externalMoment dereference the external, so voxels without one
+// answer zero here without calling them.
+static int put3f(const Vec3D<float>& f, float* out) {
+  out[0] = f.x; out[1] = f.y; out[2] = f.z;
+  return 0;
+}
+static CVX_Link* L(void* s, int l) {
+  const std::vector<CVX_Link*>& v = *S(s)->vx.linkList();
+  return l >= 0 && l < (int)v.size() ? v[l] : nullptr;
+}
+int vxr_voxel_external_force(void* s, int v, float* out3) {
+  CVX_Voxel* p = V(s, v);
+  if (!p) return -1;
+  if (!p->externalExists()) { out3[0] = out3[1] = out3[2] = 0.0f; return 0; }
+  return put3f(p->externalForce(), out3);
+}
+int vxr_voxel_external_moment(void* s, int v, float* out3) {
+  CVX_Voxel* p = V(s, v);
+  if (!p) return -1;
+  if (!p->externalExists()) { out3[0] = out3[1] = out3[2] = 0.0f; return 0; }
+  return put3f(p->externalMoment(), out3);
+}
+int vxr_voxel_corner_offset(void* s, int v, int corner, float* out3) {
+  CVX_Voxel* p = V(s, v);
+  if (!p || corner < 0 || corner > 7) return -1;
+  return put3f(p->cornerOffset((CVX_Voxel::voxelCorner)corner), out3);
+}
+int vxr_voxel_corner_position(void* s, int v, int corner, float* out3) {
+  CVX_Voxel* p = V(s, v);
+  if (!p || corner < 0 || corner > 7) return -1;
+  return put3f(p->cornerPosition((CVX_Voxel::voxelCorner)corner), out3);
+}
+int vxr_voxel_force(void* s, int v, double* out3) {
+  CVX_Voxel* p = V(s, v);
+  if (!p) return -1;
+  Vec3D<double> f = p->force();
+  out3[0] = f.x; out3[1] = f.y; out3[2] = f.z;
+  return 0;
+}
+int vxr_voxel_moment(void* s, int v, double* out3) {
+  CVX_Voxel* p = V(s, v);
+  if (!p) return -1;
+  Vec3D<double> f = p->moment();
+  out3[0] = f.x; out3[1] = f.y; out3[2] = f.z;
+  return 0;
+}
+int vxr_voxel_is_yielded(void* s, int v) { CVX_Voxel* p = V(s, v); return p ? (p->isYielded() ? 1 : 0) : -1; }
+int vxr_voxel_is_failed(void* s, int v) { CVX_Voxel* p = V(s, v); return p ? (p->isFailed() ? 1 : 0) : -1; }
+float vxr_voxel_pressure(void* s, int v) { CVX_Voxel* p = V(s, v); return p ? p->pressure() : 0.0f; }
+float vxr_link_strain_energy(void* s, int l) { CVX_Link* p = L(s, l); return p ? p->strainEnergy() : 0.0f; }
+int vxr_link_is_yielded(void* s, int l) { CVX_Link* p = L(s, l); return p ? (p->isYielded() ? 1 : 0) : -1; }
+int vxr_link_is_failed(void* s, int l) { CVX_Link* p = L(s, l); return p ? (p->isFailed() ? 1 : 0) : -1; }
+
 float vxr_state_info(void* s, int info, int type) {
   return S(s)->vx.stateInfo((CVoxelyze::stateInfoType)info, (CVoxelyze::valueType)type);
 }

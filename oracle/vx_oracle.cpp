@@ -1237,6 +1237,96 @@ struct Sim {
     for (Link& l : links) reset_link(l);
   }
 
+  // ---- per-voxel and per-link queries (VX_Voxel.h:79-130, VX_Voxel.cpp:100-159, VX_Link.cpp:127-135,
+  // 251-257) ----------------------------------------------------------------------------------
+  bool link_failed(int li) const { return li >= 0 && lmats[links[li].mat].isFailed(links[li].maxStrain); }
+  bool link_yielded(int li) const { return li >= 0 && lmats[links[li].mat].isYielded(links[li].maxStrain); }
+  // CVX_Voxel::isYielded / isFailed  VX_Voxel.cpp:92-106: any of its links
+  bool voxel_yielded(const Voxel& v) const {
+    for (int i = 0; i < 6; ++i)
+      if (link_yielded(v.links[i])) return true;
+    return false;
+  }
+  bool voxel_failed(const Voxel& v) const {
+    for (int i = 0; i < 6; ++i)
+      if (link_failed(v.links[i])) return true;
+    return false;
+  }
+  // CVX_Voxel::externalForce  VX_Voxel.cpp:117-127: the applied force, with each fixed translation
+  // replaced by the reaction -force() (computed in double, taken as float)
+  F3 external_force(const Voxel& v) const {
+    const External& e = exts[v.ext];
+    F3 r = e.force;
+    if (e.fixed(1) || e.fixed(2) || e.fixed(4)) {
+      V3 f = voxel_force(v);
+      F3 t;
+      t.x = (float)-f.x; t.y = (float)-f.y; t.z = (float)-f.z;
+      if (e.fixed(1)) r.x = t.x;
+      if (e.fixed(2)) r.y = t.y;
+      if (e.fixed(4)) r.z = t.z;
+    }
+    return r;
+  }
+  // CVX_Voxel::externalMoment  VX_Voxel.cpp:129-139
+  F3 external_moment(const Voxel& v) const {
+    const External& e = exts[v.ext];
+    F3 r = e.moment;
+    if (e.fixed(8) || e.fixed(16) || e.fixed(32)) {
+      V3 m = voxel_moment(v);
+      F3 t;
+      t.x = (float)-m.x; t.y = (float)-m.y; t.z = (float)-m.z;
+      if (e.fixed(8)) r.x = t.x;
+      if (e.fixed(16)) r.y = t.y;
+      if (e.fixed(32)) r.z = t.z;
+    }
+    return r;
+  }
+  // CVX_Voxel::cornerOffset  VX_Voxel.cpp:146-159: per axis the half-link strain of the link on the
+  // corner's side (1 without a link or with a failed one), signed, scaling half the base size
+  F3 corner_offset(const Voxel& v, int corner) const {
+    double half = 0.5 * base_size(v, 0);
+    double st[3];
+    for (int i = 0; i < 3; ++i) {
+      const bool posLink = (corner & (1 << (2 - i))) != 0;
+      const int li = v.links[2 * i + (posLink ? 0 : 1)];
+      if (li >= 0 && !link_failed(li)) st[i] = (1 + link_axial_strain(links[li], posLink)) * (posLink ? 1 : -1);
+      else st[i] = posLink ? 1.0 : -1.0;
+    }
+    F3 r;
+    r.x = (float)(half * st[0]); r.y = (float)(half * st[1]); r.z = (float)(half * st[2]);
+    return r;
+  }
+  // CVX_Voxel::cornerPosition  VX_Voxel.cpp:141-144: float position plus the offset rotated by the
+  // double orientation in the mixed-type form of Quat3D::RotateVec3D (Quat3D.h:179-186)
+  F3 corner_position(const Voxel& v, int corner) const {
+    const F3 f = corner_offset(v, corner);
+    const Q4& q = v.orient;
+    const float tw = (float)(f.x * q.x + f.y * q.y + f.z * q.z);
+    const float tx = (float)(f.x * q.w - f.y * q.z + f.z * q.y);
+    const float ty = (float)(f.x * q.z + f.y * q.w - f.z * q.x);
+    const float tz = (float)(-f.x * q.y + f.y * q.x + f.z * q.w);
+    const float rx = (float)(q.w * tx + q.x * tw + q.y * tz - q.z * ty);
+    const float ry = (float)(q.w * ty - q.x * tz + q.y * tw + q.z * tx);
+    const float rz = (float)(q.w * tz + q.x * ty - q.y * tx + q.z * tw);
+    F3 r;
+    r.x = (float)v.pos.x + rx; r.y = (float)v.pos.y + ry; r.z = (float)v.pos.z + rz;
+    return r;
+  }
+  // CVX_Voxel::pressure  VX_Voxel.h:103-104
+  float pressure(const Voxel& v) const {
+    const Material& m = vmats[v.mat];
+    F3 st = voxel_strain(v, false);
+    float vol = (float)(st.x + st.y + st.z);
+    return -m.E * vol / (3 * (1 - 2 * m.nu));
+  }
+  // CVX_Link::strainEnergy  VX_Link.cpp:251-257
+  float strain_energy(const Link& l) const {
+    const Material& m = lmats[l.mat];
+    return l.forceNeg.x * l.forceNeg.x / (2.0f * m.a1) + l.momentNeg.x * l.momentNeg.x / (2.0 * m.a2) +
+           (l.momentNeg.z * l.momentNeg.z - l.momentNeg.z * l.momentPos.z + l.momentPos.z * l.momentPos.z) / (3.0 * m.b3) +
+           (l.momentNeg.y * l.momentNeg.y - l.momentNeg.y * l.momentPos.y + l.momentPos.y * l.momentPos.y) / (3.0 * m.b3);
+  }
+
   float state_info(int info, int type) {  // Voxelyze.cpp:752-800
     float r = 0;
     if (type == 1) r = -FLT_MAX;
@@ -1253,12 +1343,9 @@ struct Sim {
       for (const Link& l : links) {
         float t = 0;
         const Material& m = lmats[l.mat];
+        (void)m;
         if (info == 7) {
-          t = l.forceNeg.x * l.forceNeg.x / (2.0f * m.a1) + l.momentNeg.x * l.momentNeg.x / (2.0 * m.a2) +
-              (l.momentNeg.z * l.momentNeg.z - l.momentNeg.z * l.momentPos.z + l.momentPos.z * l.momentPos.z) /
-                  (3.0 * m.b3) +
-              (l.momentNeg.y * l.momentNeg.y - l.momentNeg.y * l.momentPos.y + l.momentPos.y * l.momentPos.y) /
-                  (3.0 * m.b3);
+          t = strain_energy(l);
         } else if (info == 5) {
           t = l.stress;
         } else {
@@ -1298,12 +1385,7 @@ struct Sim {
             }
             break;
           }
-          case 8: {
-            F3 st = voxel_strain(v, false);
-            float vol = (float)(st.x + st.y + st.z);
-            t = -m.E * vol / (3 * (1 - 2 * m.nu));
-            break;
-          }
+          case 8: t = pressure(v); break;
           case 9: t = m.mass; break;
           default: t = 0;
         }
@@ -1589,6 +1671,51 @@ int vxo_get_link_state(void* s, double* d, float* f, int* i) {
   }
   return (int)r->links.size();
 }
+
+// ---- per-voxel and per-link queries ---------------------------------------------------------
+static int put3(const vxo::F3& f, float* out) {
+  out[0] = f.x; out[1] = f.y; out[2] = f.z;
+  return 0;
+}
+static bool valid_link(void* s, int l) { return l >= 0 && l < (int)S(s)->links.size(); }
+int vxo_voxel_external_force(void* s, int v, float* out3) {
+  if (!valid(s, v)) return -1;
+  const vxo::Voxel& x = S(s)->voxels[v];
+  if (x.ext < 0) { out3[0] = out3[1] = out3[2] = 0.0f; return 0; }
+  return put3(S(s)->external_force(x), out3);
+}
+int vxo_voxel_external_moment(void* s, int v, float* out3) {
+  if (!valid(s, v)) return -1;
+  const vxo::Voxel& x = S(s)->voxels[v];
+  if (x.ext < 0) { out3[0] = out3[1] = out3[2] = 0.0f; return 0; }
+  return put3(S(s)->external_moment(x), out3);
+}
+int vxo_voxel_corner_offset(void* s, int v, int corner, float* out3) {
+  if (!valid(s, v) || corner < 0 || corner > 7) return -1;
+  return put3(S(s)->corner_offset(S(s)->voxels[v], corner), out3);
+}
+int vxo_voxel_corner_position(void* s, int v, int corner, float* out3) {
+  if (!valid(s, v) || corner < 0 || corner > 7) return -1;
+  return put3(S(s)->corner_position(S(s)->voxels[v], corner), out3);
+}
+int vxo_voxel_force(void* s, int v, double* out3) {
+  if (!valid(s, v)) return -1;
+  vxo::V3 f = S(s)->voxel_force(S(s)->voxels[v]);
+  out3[0] = f.x; out3[1] = f.y; out3[2] = f.z;
+  return 0;
+}
+int vxo_voxel_moment(void* s, int v, double* out3) {
+  if (!valid(s, v)) return -1;
+  vxo::V3 f = S(s)->voxel_moment(S(s)->voxels[v]);
+  out3[0] = f.x; out3[1] = f.y; out3[2] = f.z;
+  return 0;
+}
+int vxo_voxel_is_yielded(void* s, int v) { return valid(s, v) ? (S(s)->voxel_yielded(S(s)->voxels[v]) ? 1 : 0) : -1; }
+int vxo_voxel_is_failed(void* s, int v) { return valid(s, v) ? (S(s)->voxel_failed(S(s)->voxels[v]) ? 1 : 0) : -1; }
+float vxo_voxel_pressure(void* s, int v) { return valid(s, v) ? S(s)->pressure(S(s)->voxels[v]) : 0.0f; }
+float vxo_link_strain_energy(void* s, int l) { return valid_link(s, l) ? S(s)->strain_energy(S(s)->links[l]) : 0.0f; }
+int vxo_link_is_yielded(void* s, int l) { return valid_link(s, l) ? (S(s)->link_yielded(l) ? 1 : 0) : -1; }
+int vxo_link_is_failed(void* s, int l) { return valid_link(s, l) ? (S(s)->link_failed(l) ? 1 : 0) : -1; }
 
 int vxo_get_collisions(void* s, int* pairs, int cap) {
   Sim* r = S(s);

@@ -226,7 +226,24 @@ def poissons_large(mk):  # tVoxelyze.h:715-768
                     s.set_displacement_all(v, (float(np.float32(1e-3)), 0.0, 0.0))
     ts = s.recommended_time_step()
     s.do_time_steps(300, ts)
-    return {"x": s.voxel_state()["pos"][s.voxel_index(4, 0, 0)][0] - 0.004, "sims": [s]}
+    # strain of the middle voxel from its corner offset (tVoxelyze.h:752-757), and the x reaction
+    # the four displaced voxels need against the stress sigma_x over the voxel's deformed cross
+    # section (:759-768), all in float as the reference computes them
+    f32 = np.float32
+    mid = s.voxel_index(4, 0, 0)
+    size = f32(2) * s.corner_offset(mid, 7)
+    strain = (size - f32(0.001)) / f32(0.001)
+    mu = f32(0.3)
+    e_hat = f32(1e6) / ((f32(1) - f32(2) * mu) * (f32(1) + mu))
+    sigma_x = e_hat * ((f32(1) - mu) * strain[0] + mu * (strain[1] + strain[2]))
+    size2 = s.corner_offset(mid, 7) - s.corner_offset(mid, 0)
+    f_x = sigma_x * f32(4) * size2[1] * size2[2]
+    total = f32(0)
+    for j in range(2):
+        for k in range(2):
+            total = total + s.external_force(s.voxel_index(8, j, k))[0]
+    return {"x": s.voxel_state()["pos"][mid][0] - 0.004, "strain": strain, "reaction_x": float(total),
+            "stress_force_x": float(f_x), "sims": [s]}
 
 
 def poissons_small(mk):  # tVoxelyze.h:689-711
@@ -295,7 +312,10 @@ def temperature(mk):  # tVoxelyze.h:989-1032
     return {"z1": z1, "z2": z2, "sims": [s]}
 
 
-def static_friction(mk):  # tVoxelyze.h:1034-1110 (first two cases)
+def static_friction(mk):  # tVoxelyze.h:1034-1110
+    """Six cases on one voxel resting on the floor: a horizontal force just below and just above
+    mu_s times the normal force, at 1 g, at 2 g, and at 1 g with mu_s = 2 (in that order, on the
+    same simulator, with resetTime between cases as the reference test does)."""
     vsize, density = 0.001, 1e3
     s = mk(vsize)
     s.enable_floor(True)
@@ -308,14 +328,19 @@ def static_friction(mk):  # tVoxelyze.h:1034-1110 (first two cases)
     s.material_set(m, F.PROP_ZETA_GLOBAL, 1.0)
     ts = s.recommended_time_step()
     xs = []
-    for factor in (0.9, 1.1):
-        s.do_time_steps(50, ts)
-        s.set_force(v, float(np.float32(factor) * np.float32(normal)), 0.0, 0.0)
-        s.do_time_steps(10, ts)
-        xs.append(s.voxel_state()["pos"][v][0])
-        s.set_force(v, 0.0, 0.0, 0.0)
-        s.reset_time()
-    return {"x_below": xs[0], "x_above": xs[1], "sims": [s]}
+    for gravity, mu_s, factors in ((1.0, None, (0.9, 1.1)), (2.0, None, (1.9, 2.1)), (1.0, 2.0, (1.9, 2.1))):
+        if gravity != 1.0 or mu_s is not None:
+            s.set_gravity(gravity)
+        if mu_s is not None:
+            s.material_set(m, F.PROP_MU_STATIC, mu_s)
+        for factor in factors:
+            s.do_time_steps(50, ts)
+            s.set_force(v, float(np.float32(factor) * np.float32(normal)), 0.0, 0.0)
+            s.do_time_steps(10, ts)
+            xs.append(s.voxel_state()["pos"][v][0])
+            s.set_force(v, 0.0, 0.0, 0.0)
+            s.reset_time()
+    return {"x_below": xs[0::2], "x_above": xs[1::2], "sims": [s]}
 
 
 def collisions(mk):  # tVoxelyze.h:1169-1197
@@ -360,14 +385,19 @@ def check_expectations(name, r):
         assert abs(3.5035e-6 - float(np.float32(r["x"]))) <= 1e-10
     elif name == "poissons_large":
         assert abs(5e-4 - float(np.float32(r["x"]))) <= 1e-7
+        assert abs(1.306e-1 - r["strain"][0]) <= 1e-3
+        assert abs(-4.048e-2 - r["strain"][1]) <= 1e-5
+        assert abs(-4.048e-2 - r["strain"][2]) <= 1e-5
+        assert abs(r["reaction_x"] - r["stress_force_x"]) <= 0.01
     elif name == "deformable_material":
         assert abs(4e-4 - float(np.float32(r["x"]))) <= 1e-7
     elif name == "temperature":
         assert abs(2.55e-5 - r["z1"]) <= 1e-8
         assert abs(-2.591e-5 - r["z2"]) <= 1e-8
     elif name == "static_friction":
-        assert r["x_below"] == 0.0
-        assert r["x_above"] != 0.0
+        assert len(r["x_below"]) == len(r["x_above"]) == 3
+        assert all(x == 0.0 for x in r["x_below"])
+        assert all(x != 0.0 for x in r["x_above"])
     elif name == "collisions":
         assert r["z"] > 0.001
 

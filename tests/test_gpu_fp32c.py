@@ -113,27 +113,32 @@ def test_fp32c_state_roundtrip_and_reset(product_lib):
     assert np.all(np.isfinite(b.voxel_state()["pos"]))
 
 
-def _fp32c(product_lib, scene, blocks_per_sm):
+def _fp32c(product_lib, scene, blocks_per_sm, split=True):
     s = make_sim(product_lib, "vx", scene)
     E = F.Engine(s)
     E.set_precision(1)
     E.set_link_pipeline(blocks_per_sm)
-    assert E.link_pipeline() == blocks_per_sm
+    E.set_link_split(split)
+    assert E.link_pipeline() == blocks_per_sm and E.link_split() == split
     return s
 
 
 @pytest.mark.parametrize("scene", ["lattice_poisson", "cantilever", "population_actuated", "graded", "floppy"])
-@pytest.mark.parametrize("blocks_per_sm", [-1, 1])
-def test_pipelined_link_pass_is_bit_identical(product_lib, scene, blocks_per_sm):
-    """The pipelined FP32C link pass (cp.async staging, resident grid) against the one-thread-per-
-    link pass: every state array identical bit for bit after each batch.  One block per SM makes
-    every block walk many tiles (both halves of the double buffer); the scenes cover Poisson's
-    ratio != 0 with bilinear materials, a fixed cantilever, in-step CTE actuation with floor and
-    friction, and one material per voxel.  The floppy beam (20 voxels in a row, E = 10 kPa) moves
-    links into and out of the large-angle branch all through the run: the pipelined pass always
-    reads each link's stored angle1v, the other pass takes it as zero while a link stays small-
-    angle, so identical states also check that the stored angle1v of a small-angle link is zero."""
+@pytest.mark.parametrize("variant", ["pipelined_all", "pipelined_1", "general"])
+def test_link_pass_variants_are_bit_identical(product_lib, scene, variant):
+    """The FP32C link-pass variants against the default split pass (a small-angle kernel, then the
+    general kernel over the links it deferred): every state array identical bit for bit after each
+    batch.  Variants: the pipelined pass (cp.async staging, resident grid; one block per SM makes
+    every block walk many tiles, both halves of the double buffer) and the general one-thread-per-
+    link pass.  The scenes cover Poisson's ratio != 0 with bilinear materials, a fixed cantilever,
+    in-step CTE actuation with floor and friction, and one material per voxel.  The floppy beam (20
+    voxels in a row, E = 10 kPa) moves links into and out of the large-angle branch all through the
+    run, so the split pass defers links every step: the pipelined pass always reads each link's
+    stored angle1v, the small-angle kernel takes it as zero, so identical states also check that
+    the stored angle1v of a small-angle link is zero."""
     from conftest import state_diff
+
+    blocks_per_sm = {"pipelined_all": -1, "pipelined_1": 1, "general": 0}[variant]
 
     sc = {"lattice_poisson": lambda: S.lattice(40, 36, 20),
           "cantilever": lambda: S.cantilever(40, 8, 8),
@@ -141,7 +146,7 @@ def test_pipelined_link_pass_is_bit_identical(product_lib, scene, blocks_per_sm)
           "graded": lambda: S.graded_population(6, 10),
           "floppy": lambda: S.cantilever(20, 1, 1, E=1e4, tip_force=-0.02)}[scene]()
     a = _fp32c(product_lib, sc, 0)
-    b = _fp32c(product_lib, sc, blocks_per_sm)
+    b = _fp32c(product_lib, sc, blocks_per_sm, split=variant != "general")
     dt = a.recommended_time_step()
     assert b.recommended_time_step() == dt
     if scene in ("population_actuated", "graded"):

@@ -1462,6 +1462,60 @@ int vx_state_info_into(void* s, int info, int type, float* d_out, const char** w
   }
   return vxg_reduce_fixed(I.eng, info, type, d_out, why);
 }
+// per-voxel and per-link queries (VX_Voxel.h:79-130, VX_Link.h:47-66) on the host mirror, which
+// the first read after a step downloads.  A voxel without an external answers zero for its
+// external force and moment (the reference dereferences the missing external there).
+static int put3f(const Vec3D<float>& f, float* out) {
+  out[0] = f.x; out[1] = f.y; out[2] = f.z;
+  return 0;
+}
+static CVX_Link* Lk(void* s, int l) {
+  CVoxelyze& vx = H(s)->vx;
+  return l >= 0 && l < vx.linkCount() ? vx.link(l) : nullptr;
+}
+int vx_voxel_external_force(void* s, int v, float* out3) {
+  CVX_Voxel* p = Vx(s, v);
+  if (!p || !out3) return -1;
+  if (!p->externalExists()) { out3[0] = out3[1] = out3[2] = 0.0f; return 0; }
+  return put3f(p->externalForce(), out3);
+}
+int vx_voxel_external_moment(void* s, int v, float* out3) {
+  CVX_Voxel* p = Vx(s, v);
+  if (!p || !out3) return -1;
+  if (!p->externalExists()) { out3[0] = out3[1] = out3[2] = 0.0f; return 0; }
+  return put3f(p->externalMoment(), out3);
+}
+int vx_voxel_corner_offset(void* s, int v, int corner, float* out3) {
+  CVX_Voxel* p = Vx(s, v);
+  if (!p || !out3 || corner < 0 || corner > 7) return -1;
+  return put3f(p->cornerOffset((CVX_Voxel::voxelCorner)corner), out3);
+}
+int vx_voxel_corner_position(void* s, int v, int corner, float* out3) {
+  CVX_Voxel* p = Vx(s, v);
+  if (!p || !out3 || corner < 0 || corner > 7) return -1;
+  return put3f(p->cornerPosition((CVX_Voxel::voxelCorner)corner), out3);
+}
+int vx_voxel_force(void* s, int v, double* out3) {
+  CVX_Voxel* p = Vx(s, v);
+  if (!p || !out3) return -1;
+  Vec3D<double> f = p->force();
+  out3[0] = f.x; out3[1] = f.y; out3[2] = f.z;
+  return 0;
+}
+int vx_voxel_moment(void* s, int v, double* out3) {
+  CVX_Voxel* p = Vx(s, v);
+  if (!p || !out3) return -1;
+  Vec3D<double> f = p->moment();
+  out3[0] = f.x; out3[1] = f.y; out3[2] = f.z;
+  return 0;
+}
+int vx_voxel_is_yielded(void* s, int v) { CVX_Voxel* p = Vx(s, v); return p ? (p->isYielded() ? 1 : 0) : -1; }
+int vx_voxel_is_failed(void* s, int v) { CVX_Voxel* p = Vx(s, v); return p ? (p->isFailed() ? 1 : 0) : -1; }
+float vx_voxel_pressure(void* s, int v) { CVX_Voxel* p = Vx(s, v); return p ? p->pressure() : 0.0f; }
+float vx_link_strain_energy(void* s, int l) { CVX_Link* p = Lk(s, l); return p ? p->strainEnergy() : 0.0f; }
+int vx_link_is_yielded(void* s, int l) { CVX_Link* p = Lk(s, l); return p ? (p->isYielded() ? 1 : 0) : -1; }
+int vx_link_is_failed(void* s, int l) { CVX_Link* p = Lk(s, l); return p ? (p->isFailed() ? 1 : 0) : -1; }
+
 int vx_counters(void* s, long long* out, int n) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.impl()->eng) return -1;
@@ -1533,6 +1587,16 @@ int vx_set_link_pipeline(void* s, int blocks_per_sm) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.upload()) return -1;
   return vxg_set_link_pipeline(vx.impl()->eng, blocks_per_sm) ? -1 : 0;
+}
+int vx_set_link_split(void* s, int on) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_set_link_split(vx.impl()->eng, on) ? -1 : 0;
+}
+int vx_get_link_split(void* s, int* on) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_get_link_split(vx.impl()->eng, on) ? -1 : 0;
 }
 int vx_set_poisson_fusion(void* s, int on) {
   CVoxelyze& vx = H(s)->vx;

@@ -74,6 +74,18 @@ _SIGS = {
     "get_link_state": (_i, [_p, _dp, _fp, _ip]),
     "get_collisions": (_i, [_p, _ip, _i]),
     "state_info": (_f, [_p, _i, _i]),
+    "voxel_external_force": (_i, [_p, _i, _fp]),
+    "voxel_external_moment": (_i, [_p, _i, _fp]),
+    "voxel_corner_offset": (_i, [_p, _i, _i, _fp]),
+    "voxel_corner_position": (_i, [_p, _i, _i, _fp]),
+    "voxel_force": (_i, [_p, _i, _dp]),
+    "voxel_moment": (_i, [_p, _i, _dp]),
+    "voxel_is_yielded": (_i, [_p, _i]),
+    "voxel_is_failed": (_i, [_p, _i]),
+    "voxel_pressure": (_f, [_p, _i]),
+    "link_strain_energy": (_f, [_p, _i]),
+    "link_is_yielded": (_i, [_p, _i]),
+    "link_is_failed": (_i, [_p, _i]),
 }
 
 
@@ -285,6 +297,68 @@ class Sim:
     def state_info(self, info: int, vtype: int) -> float:
         return self.f["state_info"](self.h, info, vtype)
 
+    # -- per-voxel and per-link queries (VX_Voxel.h:79-130, VX_Link.h:47-66) -----------------
+    def _vec(self, name, ct, *args) -> np.ndarray:
+        out = np.zeros(3, np.float32 if ct is C.c_float else np.float64)
+        if self.f[name](self.h, *args, _ptr(out, ct)) != 0:
+            raise IndexError(f"{name}{args}")
+        return out
+
+    def external_force(self, v: int) -> np.ndarray:
+        """CVX_Voxel::externalForce: applied force, reaction force on fixed translations."""
+        return self._vec("voxel_external_force", C.c_float, v)
+
+    def external_moment(self, v: int) -> np.ndarray:
+        return self._vec("voxel_external_moment", C.c_float, v)
+
+    def corner_offset(self, v: int, corner: int) -> np.ndarray:
+        return self._vec("voxel_corner_offset", C.c_float, v, corner)
+
+    def corner_position(self, v: int, corner: int) -> np.ndarray:
+        return self._vec("voxel_corner_position", C.c_float, v, corner)
+
+    def voxel_force(self, v: int) -> np.ndarray:
+        return self._vec("voxel_force", C.c_double, v)
+
+    def voxel_moment(self, v: int) -> np.ndarray:
+        return self._vec("voxel_moment", C.c_double, v)
+
+    def voxel_is_yielded(self, v: int) -> bool:
+        return self.f["voxel_is_yielded"](self.h, v) == 1
+
+    def voxel_is_failed(self, v: int) -> bool:
+        return self.f["voxel_is_failed"](self.h, v) == 1
+
+    def pressure(self, v: int) -> float:
+        return self.f["voxel_pressure"](self.h, v)
+
+    def strain_energy(self, l: int) -> float:
+        return self.f["link_strain_energy"](self.h, l)
+
+    def link_is_yielded(self, l: int) -> bool:
+        return self.f["link_is_yielded"](self.h, l) == 1
+
+    def link_is_failed(self, l: int) -> bool:
+        return self.f["link_is_failed"](self.h, l) == 1
+
+    def queries(self, corners=range(8)) -> dict:
+        """Every per-voxel and per-link query for the whole scene, as arrays (for comparisons)."""
+        nv, nl = self.voxel_count(), self.link_count()
+        return {
+            "external_force": np.array([self.external_force(v) for v in range(nv)]).reshape(nv, 3),
+            "external_moment": np.array([self.external_moment(v) for v in range(nv)]).reshape(nv, 3),
+            "corner_offset": np.array([[self.corner_offset(v, c) for c in corners] for v in range(nv)]),
+            "corner_position": np.array([[self.corner_position(v, c) for c in corners] for v in range(nv)]),
+            "voxel_yielded": np.array([self.voxel_is_yielded(v) for v in range(nv)]),
+            "voxel_failed": np.array([self.voxel_is_failed(v) for v in range(nv)]),
+            "pressure": np.array([self.pressure(v) for v in range(nv)], np.float32),
+            "strain_energy": np.array([self.strain_energy(l) for l in range(nl)], np.float32),
+            "link_yielded": np.array([self.link_is_yielded(l) for l in range(nl)]),
+            "link_failed": np.array([self.link_is_failed(l) for l in range(nl)]),
+            "force": np.array([self.voxel_force(v) for v in range(nv)]).reshape(nv, 3),
+            "moment": np.array([self.voxel_moment(v) for v in range(nv)]).reshape(nv, 3),
+        }
+
     # -- readback --------------------------------------------------------------------------
     def voxel_state(self) -> dict:
         n = self.voxel_count()
@@ -334,6 +408,8 @@ _EXT_SIGS = {
     "autotune": (_i, [_p, _i, _f, _ip]),
     "set_link_pipeline": (_i, [_p, _i]),
     "get_link_pipeline": (_i, [_p, _ip]),
+    "set_link_split": (_i, [_p, _i]),
+    "get_link_split": (_i, [_p, _ip]),
     "set_decisions": (_i, [_p, _i, C.c_longlong]),
     "get_decisions": (_i, [_p, C.POINTER(C.c_ubyte), C.c_longlong]),
     "put_decisions": (_i, [_p, C.POINTER(C.c_ubyte), C.c_longlong]),
@@ -389,6 +465,16 @@ class Engine:
         """FP32C link pass: >0 pipelined kernel with that many resident blocks per SM, -1 as many
         as fit, 0 the one-thread-per-link kernel (default)."""
         self._ck(self.f["set_link_pipeline"](self.sim.h, blocks_per_sm))
+
+    def set_link_split(self, on: bool):
+        """FP32C link pass at a fixed dt: the small-angle kernel plus the general kernel over the
+        links it defers (default), or the general kernel over every link; identical results."""
+        self._ck(self.f["set_link_split"](self.sim.h, 1 if on else 0))
+
+    def link_split(self) -> bool:
+        out = np.zeros(1, np.int32)
+        self._ck(self.f["get_link_split"](self.sim.h, _ptr(out, C.c_int)))
+        return bool(out[0])
 
     def set_poisson_fusion(self, on: bool):
         """FP32C, nu != 0: fill the Poisson-strain cache in the voxel pass (default) or in a

@@ -88,12 +88,15 @@ def measured_traffic(kind: str, n_voxels: int, n_links: int):
 
 
 # FP64 path against the FP64 pipe.  Double-precision instructions per unit counted by ncu
-# (sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum and sm__inst_executed_pipe_fp64.sum,
-# one launch of each pass of the FP64 path after warm-up) on the bench's lattice generator, divided by
-# the units of the launch.  FLOPs count an FMA as two.  None until measured.
+# (sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum and sm__inst_executed_pipe_fp64.sum)
+# on a warm launch of each pass of the FP64 path on the bench's lattice generator at 48x48x24
+# (46,964 voxels, 116,312 links), divided by the units of the launch
+# (profiles/fp64_k_link_k_voxel_lattice48x48x24_counts.md).  The DFMAs are the iterations of IEEE
+# division and square root (the FP64 path is compiled without contraction); their count varies by
+# ~20 % between steps with the operands.  FLOPs count an FMA as two.
 FP64_OPS = {
-    "link": None,   # {"dadd": .., "dmul": .., "dfma": .., "pipe_warp_inst": ..} per link
-    "voxel": None,  # the same per voxel
+    "link": {"dadd": 136.65, "dmul": 142.01, "dfma": 21.06, "pipe_warp_inst": 11.594},
+    "voxel": {"dadd": 104.09, "dmul": 115.04, "dfma": 14.42, "pipe_warp_inst": 8.298},
 }
 
 
