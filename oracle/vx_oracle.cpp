@@ -832,19 +832,60 @@ struct Sim {
     cols.clear();
     for (Voxel& v : voxels) v.colWatch.clear();
   }
+  // CVoxelyze::regenerateCollisions  Voxelyze.cpp:725-750.  The reference tests every later voxel
+  // j > i for each surface voxel i (O(N^2)); the same pairs come from a grid of cells slightly
+  // wider than the watch radius, so that every j within the radius lies in one of the 27 cells
+  // around i's, each candidate then passing the reference's exact double-precision distance test
+  // and nearby exclusion.  Pairs are listed in (i, j) order as the reference's loops produce them,
+  // and each voxel's watch list in that list order, so the result is the reference's.
   void regenerate_collisions(float thr) {
     clear_collisions();
-    int n = (int)voxels.size();
+    const int n = (int)voxels.size();
+    const double h = std::sqrt((double)thr) * 1.001 + 1e-300;
+    std::unordered_map<Key, std::vector<int>, KeyHash> cell;
+    auto key_of = [&](const V3& p) {
+      Key k;
+      k.x = (int)std::floor(p.x / h); k.y = (int)std::floor(p.y / h); k.z = (int)std::floor(p.z / h);
+      return k;
+    };
+    std::vector<int> surf;
     for (int i = 0; i < n; ++i) {
       Voxel& a = voxels[i];
       if (a.interior) continue;
       a.lastColWatch.x = (float)a.pos.x; a.lastColWatch.y = (float)a.pos.y; a.lastColWatch.z = (float)a.pos.z;
-      for (int j = i + 1; j < n; ++j) {
+      cell[key_of(a.pos)].push_back(i);  // ascending i within each cell
+      surf.push_back(i);
+    }
+    std::vector<std::vector<int>> partners(surf.size());
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+    for (long long si = 0; si < (long long)surf.size(); ++si) {
+      const int i = surf[si];
+      const Voxel& a = voxels[i];
+      const Key c = key_of(a.pos);
+      std::vector<int>& out = partners[si];
+      for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            Key k;
+            k.x = c.x + dx; k.y = c.y + dy; k.z = c.z + dz;
+            auto it = cell.find(k);
+            if (it == cell.end()) continue;
+            for (int j : it->second) {
+              if (j <= i) continue;
+              const Voxel& b = voxels[j];
+              double ex = a.pos.x - b.pos.x, ey = a.pos.y - b.pos.y, ez = a.pos.z - b.pos.z;
+              if (ex * ex + ey * ey + ez * ez > thr) continue;
+              if (std::binary_search(a.nearby.begin(), a.nearby.end(), j)) continue;
+              out.push_back(j);
+            }
+          }
+      std::sort(out.begin(), out.end());
+    }
+    for (size_t si = 0; si < surf.size(); ++si) {
+      const int i = surf[si];
+      for (int j : partners[si]) {
+        Voxel& a = voxels[i];
         Voxel& b = voxels[j];
-        if (b.interior) continue;
-        double dx = a.pos.x - b.pos.x, dy = a.pos.y - b.pos.y, dz = a.pos.z - b.pos.z;
-        if (dx * dx + dy * dy + dz * dz > thr) continue;
-        if (std::binary_search(a.nearby.begin(), a.nearby.end(), j)) continue;
         const Material& m1 = vmats[a.mat];
         const Material& m2 = vmats[b.mat];
         Collision c;
@@ -889,6 +930,8 @@ struct Sim {
     float watchMm = (float)(voxSize * watchVx);
     float recalc = (float)(voxSize * watchDistance / 2);
     if (nearbyStale) {
+      // each voxel's list depends on the lattice only
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 256)
       for (int v = 0; v < (int)voxels.size(); ++v) generate_nearby(v, (int)(watchVx * 2));
       nearbyStale = false;
       collisionsStale = true;
@@ -899,7 +942,8 @@ struct Sim {
       if (dx * dx + dy * dy + dz * dz > recalc * recalc) collisionsStale = true;
     }
     if (collisionsStale) regenerate_collisions(watchMm * watchMm);
-    for (Collision& c : cols) update_contact(c);
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+    for (long long k = 0; k < (long long)cols.size(); ++k) update_contact(cols[k]);
   }
 
   // ---- scene building (Voxelyze.cpp:357-640) ---------------------------------------------
@@ -1191,7 +1235,11 @@ struct Sim {
   // Serial-equivalent Poisson strain pre-pass: the first link of each nu != 0 voxel would fill the
   // cache from the previous step's link strains (VX_Voxel.cpp:336-343, VX_Link.cpp:160).
   void poisson_prepass() {
-    for (Voxel& v : voxels) {
+    // each voxel's cache reads only the previous step's link strains and writes only itself
+    const int nv = (int)voxels.size();
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+    for (int k = 0; k < nv; ++k) {
+      Voxel& v = voxels[k];
       if (!v.pStrainInvalid || vmats[v.mat].nu == 0) continue;
       bool any = false;
       for (int i = 0; i < 6; ++i) any |= v.links[i] >= 0;
