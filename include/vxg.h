@@ -216,10 +216,10 @@ int vxg_get_launch(vxg_engine* e, int* block_link, int* block_voxel, int* graph_
  * Both give identical results. */
 int vxg_set_link_pipeline(vxg_engine* e, int blocks_per_sm);
 int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm);
-/* FP32C link pass at a fixed dt, one thread per link: on (1, the default) a small-angle kernel runs
- * every link that stays in CVX_Link::orientLink's small-angle branch (src/VX_Link.cpp:92-110) and a
- * general kernel the links it deferred (large-angle, or leaving the branch this step); off (0) the
- * general kernel runs every link.  Results are bit-identical either way.  vxg_autotune compares
+/* FP32C link pass at a fixed dt, one thread per link: on (1) a small-angle kernel runs every link
+ * that stays in CVX_Link::orientLink's small-angle branch (src/VX_Link.cpp:92-110) and a general
+ * kernel the links it deferred (large-angle, or leaving the branch this step); off (0, the default)
+ * the general kernel runs every link.  Results are bit-identical either way.  vxg_autotune compares
  * both. */
 int vxg_set_link_split(vxg_engine* e, int on);
 int vxg_get_link_split(vxg_engine* e, int* on);

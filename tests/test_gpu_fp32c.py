@@ -126,11 +126,11 @@ def _fp32c(product_lib, scene, blocks_per_sm, split=True):
 @pytest.mark.parametrize("scene", ["lattice_poisson", "cantilever", "population_actuated", "graded", "floppy"])
 @pytest.mark.parametrize("variant", ["pipelined_all", "pipelined_1", "general"])
 def test_link_pass_variants_are_bit_identical(product_lib, scene, variant):
-    """The FP32C link-pass variants against the default split pass (a small-angle kernel, then the
-    general kernel over the links it deferred): every state array identical bit for bit after each
-    batch.  Variants: the pipelined pass (cp.async staging, resident grid; one block per SM makes
-    every block walk many tiles, both halves of the double buffer) and the general one-thread-per-
-    link pass.  The scenes cover Poisson's ratio != 0 with bilinear materials, a fixed cantilever,
+    """The FP32C link-pass variants against the split pass (a small-angle kernel, then the general
+    kernel over the links it deferred): every state array identical bit for bit after each batch.
+    Variants: the pipelined pass (cp.async staging, resident grid; one block per SM makes every
+    block walk many tiles, both halves of the double buffer) and the general one-thread-per-link
+    pass (the default).  The scenes cover Poisson's ratio != 0 with bilinear materials, a fixed cantilever,
     in-step CTE actuation with floor and friction, and one material per voxel.  The floppy beam (20
     voxels in a row, E = 10 kPa) moves links into and out of the large-angle branch all through the
     run, so the split pass defers links every step: the pipelined pass always reads each link's

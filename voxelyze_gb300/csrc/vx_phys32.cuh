@@ -508,10 +508,12 @@ VX_HD void voxel_gather_own(const View& S, int v, VoxIn& in) {
 
 // FUSE_POIS: fill the Poisson-strain cache for the next step's link pass here, from this step's
 // link strains (which no later kernel of the step changes), instead of in a separate pre-pass
+// dOut / cOut (optional): the voxel's displacement and its compensation after the step.
 template <bool FUSE_POIS>
-VX_HDN void voxel_step(const View& S, int v, float dt, const VoxIn& in) {
+VX_HDN void voxel_step(const View& S, int v, float dt, const VoxIn& in, f3* dOut = nullptr, f3* cOut = nullptr) {
   const vx64::View& B = S.B;
   const int nv = B.nv, nl = B.nl;
+  if (dOut) { *dOut = in.d; *cOut = in.c; }
   if (dt == 0.0f) return;
   const vxg_voxel_material& m = B.vm[in.vmat];
   int ei = in.ei;
@@ -519,6 +521,7 @@ VX_HDN void voxel_step(const View& S, int v, float dt, const VoxIn& in) {
   if (e && (e->dof & 0x3F) == 0x3F) {
     S.P[v] = make_float4((float)e->translation[0], (float)e->translation[1], (float)e->translation[2], 0.0f);
     st3(S.c, nv, v, F3(0, 0, 0));
+    if (dOut) { *dOut = F3((float)e->translation[0], (float)e->translation[1], (float)e->translation[2]); *cOut = F3(0, 0, 0); }
     S.Q[v] = make_float4((float)e->rotq[0], (float)e->rotq[1], (float)e->rotq[2], (float)e->rotq[3]);
     stq(S.qc, nv, v, Q4(0, 0, 0, 0));
     st3(S.lin, nv, v, F3(0, 0, 0));
@@ -648,6 +651,7 @@ VX_HDN void voxel_step(const View& S, int v, float dt, const VoxIn& in) {
   }
   S.P[v] = make_float4(d.x, d.y, d.z, 0.0f);
   st3(S.c, nv, v, c);
+  if (dOut) { *dOut = d; *cOut = c; }
   st3(S.lin, nv, v, lin);
   st3(S.ang, nv, v, ang);
   S.Q[v] = make_float4(q.w, q.x, q.y, q.z);

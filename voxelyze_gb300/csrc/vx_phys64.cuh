@@ -103,6 +103,13 @@ struct View {
   const int* colOff;   // nv + 1
   const int* colItem;  // collision index * 2 + (voxel is the second of the pair)
   const float* colForce; // 3 per collision
+  // collisions on: the voxel pass votes whether any surface voxel moved past the rebuild distance
+  // from its position at the last rebuild (colLast), for the next step's collision stage (colVote
+  // is null when collisions are off)
+  int* colVote;
+  const float* colLast;  // 3 nv
+  double colRecalc2;     // rebuild distance squared
+  double colS;           // voxel size (FP32C positions: lattice index * colS + displacement)
   Ctl* ctl;
 };
 

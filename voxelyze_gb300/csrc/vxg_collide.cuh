@@ -2,8 +2,13 @@
 // CVX_Collision::updateContactForce (src/Voxelyze.cpp:670-750, src/VX_Collision.cpp:15-56).
 //
 // Per step, on the engine stream:
-//   c_check    each surface voxel tests its drift from the position at the last rebuild (float
-//              copy, double distance, as the reference) and raises the device "stale" flag
+//   c_surface  once per batch: the surface voxels as a list (warp ballot, one atomic per warp),
+//              the only voxels the stale test and the rebuild visit
+//   c_check    the first step of a batch (or of a captured chunk): each surface voxel tests its
+//              drift from the position at the last rebuild (float copy, double distance, as the
+//              reference) and raises the device "stale" flag; every later step takes the vote the
+//              previous step's voxel pass cast from the positions it wrote (the same test on the
+//              same numbers)
 //   rebuild    only when stale (it exits at once otherwise); one cooperative launch (c_rebuild)
 //              runs these phases with grid-wide barriers between them, or, where cooperative
 //              launches are not available, six separate kernels:
@@ -29,6 +34,8 @@ struct ColCtl {
   int nwatch;
   int status;       // overflow bits
   int rebuilds;
+  int vote;         // set by a voxel pass whose new positions make the pair list stale
+  int nsurf;        // surface voxels listed by c_surface
 };
 
 enum { VXG_COL_ST_PAIR_OVERFLOW = 1, VXG_COL_ST_WATCH_OVERFLOW = 2, VXG_COL_ST_LOCAL_OVERFLOW = 4,
@@ -61,6 +68,7 @@ struct ColView {
   int* next;                 // nv
   int* cntGt;                // nv
   int* cntAll;               // nv
+  int* surf;                 // nv: the surface voxels (c_surface), nsurf of them
   int* pairOff;              // nv + 1
   int* watchOff;             // nv + 1
   int* watchPartner;         // wcap
@@ -110,11 +118,42 @@ __device__ __forceinline__ bool c_moved(const ColView& C, int v) {
          dz = cpos(C, v, 2) - C.lastWatch[2 * C.nv + v];
   return dx * dx + dy * dy + dz * dz > C.recalc2;
 }
-__global__ void c_check(ColView C) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
+// The surface voxels as a dense list: a warp ballot of the interior flags, one atomic per warp for
+// the list slots.  The list's order varies from run to run; every use of it writes per voxel (and
+// the rebuild sorts what it collects), so results do not depend on it.  Interior voxels' partner
+// counts are zeroed here, since the rebuild visits listed voxels only.
+__global__ void c_surface(ColView C) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = v < C.nv;
+  const bool surf = live && is_surface(C, v);
+  if (live && !surf) {
+    C.cntAll[v] = 0;
+    C.cntGt[v] = 0;
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, surf);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&C.cc->nsurf, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (surf) C.surf[base + __popc(m & ((1u << lane) - 1u))] = v;
+}
+// first step of a batch: the full stale test over the surface list; later steps: the voxel pass's
+// vote.  Either way the vote is cleared for the step's own voxel pass.
+__device__ __forceinline__ bool c_moved_listed(const ColView& C, int first, int stride) {
+  bool moved = false;
+  const int n = C.cc->nsurf;
+  for (int i = first; i < n; i += stride) moved |= c_moved(C, C.surf[i]);
+  return moved;
+}
+__global__ void c_check(ColView C, int full) {
   if (C.ctl->halt || C.ctl->diverged) return;  // the same for the whole launch
-  if (v == 0 && C.cc->force_stale) C.cc->stale = 1;
-  if (__syncthreads_or(c_moved(C, v)) && threadIdx.x == 0) C.cc->stale = 1;
+  const int first = blockIdx.x * blockDim.x + threadIdx.x;
+  if (first == 0) {
+    if (C.cc->force_stale || (!full && C.cc->vote)) C.cc->stale = 1;
+    C.cc->vote = 0;
+  }
+  if (full && __syncthreads_or(c_moved_listed(C, first, gridDim.x * blockDim.x)) && threadIdx.x == 0) C.cc->stale = 1;
 }
 
 // rebuild only when c_check found the list stale and the step has not diverged (the same for
@@ -159,7 +198,8 @@ __device__ void c_insert_one(const ColView& C, int v) {
   atomicOr(&C.cc->status, VXG_COL_ST_HASH_FULL);
 }
 __global__ void c_insert(ColView C) {
-  if (c_rebuilding(C)) c_insert_one(C, blockIdx.x * blockDim.x + threadIdx.x);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c_rebuilding(C) && i < C.cc->nsurf) c_insert_one(C, C.surf[i]);
 }
 
 __device__ __forceinline__ int find_cell(const ColView& C, unsigned long long k) {
@@ -213,7 +253,8 @@ __device__ void c_count_one(const ColView& C, int v) {
   C.cntGt[v] = gt;
 }
 __global__ void c_count(ColView C) {
-  if (c_rebuilding(C)) c_count_one(C, blockIdx.x * blockDim.x + threadIdx.x);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c_rebuilding(C) && i < C.cc->nsurf) c_count_one(C, C.surf[i]);
 }
 
 // exclusive scans of cntGt -> pairOff and cntAll -> watchOff by one block of up to 1024 threads
@@ -289,7 +330,8 @@ __device__ void c_fill_one(const ColView& C, int v) {
   }
 }
 __global__ void c_fill(ColView C) {
-  if (c_rebuilding(C) && !C.cc->status) c_fill_one(C, blockIdx.x * blockDim.x + threadIdx.x);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c_rebuilding(C) && !C.cc->status && i < C.cc->nsurf) c_fill_one(C, C.surf[i]);
 }
 
 __device__ void c_watch_one(const ColView& C, int v) {
@@ -316,7 +358,8 @@ __device__ void c_watch_one(const ColView& C, int v) {
   }
 }
 __global__ void c_watch(ColView C) {
-  if (c_rebuilding(C) && !C.cc->status) c_watch_one(C, blockIdx.x * blockDim.x + threadIdx.x);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c_rebuilding(C) && !C.cc->status && i < C.cc->nsurf) c_watch_one(C, C.surf[i]);
 }
 
 // The whole rebuild in one cooperative launch: the phases above, separated by grid-wide barriers
@@ -326,19 +369,20 @@ __global__ void __launch_bounds__(256) c_rebuild(ColView C) {
   if (!c_rebuilding(C)) return;  // uniform: no block reaches a barrier unless all do
   cooperative_groups::grid_group grid = cooperative_groups::this_grid();
   const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  const int ns = C.cc->nsurf;
   c_clear_range(C, first, stride);
   grid.sync();
-  for (int v = first; v < C.nv; v += stride) c_insert_one(C, v);
+  for (int i = first; i < ns; i += stride) c_insert_one(C, C.surf[i]);
   grid.sync();
-  for (int v = first; v < C.nv; v += stride) c_count_one(C, v);
+  for (int i = first; i < ns; i += stride) c_count_one(C, C.surf[i]);
   grid.sync();
   if (blockIdx.x == 0) c_scan_block(C);
   grid.sync();
   if (C.cc->status) return;  // written before the last barrier: the same for every block
-  for (int v = first; v < C.nv; v += stride) c_fill_one(C, v);
+  for (int i = first; i < ns; i += stride) c_fill_one(C, C.surf[i]);
   grid.sync();
   if (C.cc->status) return;
-  for (int v = first; v < C.nv; v += stride) c_watch_one(C, v);
+  for (int i = first; i < ns; i += stride) c_watch_one(C, C.surf[i]);
 }
 
 // CVX_Voxel::baseSizeAverage for the envelope  VX_Voxel.h:90
@@ -423,29 +467,33 @@ __global__ void c_contact(ColView C) {
 // list stale, the contact forces, separated by grid-wide barriers (a cooperative launch keeps
 // every block resident, so the barriers end; every branch around a barrier reads words that
 // were written before the previous barrier, so all blocks take it alike).
-__global__ void __launch_bounds__(256) c_stage(ColView C) {
+// full: the first step of a batch (the stale test over the surface list); otherwise the vote of
+// the previous step's voxel pass decides.
+__global__ void __launch_bounds__(256) c_stage(ColView C, int full) {
   if (C.ctl->halt || C.ctl->diverged) return;  // uniform: set before this launch
   cooperative_groups::grid_group grid = cooperative_groups::this_grid();
   const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-  bool moved = false;
-  for (int v = first; v < C.nv; v += stride) moved |= c_moved(C, v);
-  if (first == 0 && C.cc->force_stale) C.cc->stale = 1;
-  if (__syncthreads_or(moved) && threadIdx.x == 0) C.cc->stale = 1;
+  const int ns = C.cc->nsurf;
+  if (first == 0) {
+    if (C.cc->force_stale || (!full && C.cc->vote)) C.cc->stale = 1;
+    C.cc->vote = 0;
+  }
+  if (full && __syncthreads_or(c_moved_listed(C, first, stride)) && threadIdx.x == 0) C.cc->stale = 1;
   grid.sync();
   if (C.cc->stale) {
     c_clear_range(C, first, stride);
     grid.sync();
-    for (int v = first; v < C.nv; v += stride) c_insert_one(C, v);
+    for (int i = first; i < ns; i += stride) c_insert_one(C, C.surf[i]);
     grid.sync();
-    for (int v = first; v < C.nv; v += stride) c_count_one(C, v);
+    for (int i = first; i < ns; i += stride) c_count_one(C, C.surf[i]);
     grid.sync();
     if (blockIdx.x == 0) c_scan_block(C);
     grid.sync();
     if (!C.cc->status)
-      for (int v = first; v < C.nv; v += stride) c_fill_one(C, v);
+      for (int i = first; i < ns; i += stride) c_fill_one(C, C.surf[i]);
     grid.sync();
     if (!C.cc->status)
-      for (int v = first; v < C.nv; v += stride) c_watch_one(C, v);
+      for (int i = first; i < ns; i += stride) c_watch_one(C, C.surf[i]);
     grid.sync();
   }
   c_contact_all(C, first, stride);
@@ -525,6 +573,7 @@ struct Collide {
     size_t o_last = take(sizeof(float) * 3 * (size_t)n);
     size_t o_hkey = take(8 * hcap), o_hhead = take(4 * hcap);
     size_t o_next = take(4 * (size_t)n), o_cg = take(4 * (size_t)n), o_ca = take(4 * (size_t)n);
+    size_t o_surf = take(4 * (size_t)n);
     size_t o_po = take(4 * ((size_t)n + 1)), o_wo = take(4 * ((size_t)n + 1));
     size_t o_wp = take(4 * (size_t)wcap), o_wi = take(4 * (size_t)wcap);
     size_t o_pi = take(4 * (size_t)pcap), o_pj = take(4 * (size_t)pcap), o_ps = take(4 * (size_t)pcap),
@@ -541,6 +590,7 @@ struct Collide {
     C.next = (int*)(buf + o_next);
     C.cntGt = (int*)(buf + o_cg);
     C.cntAll = (int*)(buf + o_ca);
+    C.surf = (int*)(buf + o_surf);
     C.pairOff = (int*)(buf + o_po);
     C.watchOff = (int*)(buf + o_wo);
     C.watchPartner = (int*)(buf + o_wp);
@@ -600,6 +650,24 @@ struct Collide {
     S.colOff = C.watchOff;
     S.colItem = C.watchItem;
     S.colForce = C.pairForce;
+    S.colVote = nullptr;  // set per launch when collisions are on (voted())
+    S.colLast = C.lastWatch;
+  }
+  // the View a voxel pass gets when collisions are on: it votes for the next step's stage
+  bool ready() const { return buf && C.nbOff; }
+  void voted(View& S, const vxg_globals& g) {
+    set_globals(g);
+    S.colVote = ready() ? &cc->vote : nullptr;
+    S.colLast = C.lastWatch;
+    S.colRecalc2 = C.recalc2;
+    S.colS = C.s64;
+  }
+  // once per batch: the surface list the stage walks
+  int enqueue_surface(cudaStream_t s) {
+    if (!ready()) return 0;
+    cudaMemsetAsync(&cc->nsurf, 0, sizeof(int), s);
+    c_surface<<<std::max(1, (nv + 255) / 256), 256, 0, s>>>(C);
+    return 1;
   }
   void set_globals(const vxg_globals& g) {
     float watchVx = 2 * g.boundingRadius + g.watchDistance;
@@ -664,18 +732,21 @@ struct Collide {
     }
     return stage_blocks;
   }
-  int enqueue(const vxg_globals& g, cudaStream_t s) {
+  // full: the stale test itself (the first step of a batch or captured chunk); otherwise the vote
+  // of the previous step's voxel pass
+  int enqueue(const vxg_globals& g, cudaStream_t s, bool full) {
     if (!buf || !C.nbOff) return 0;
     set_globals(g);
+    int fl = full ? 1 : 0;
     const int gs = stage_grid();
     if (gs > 0) {
-      void* args[] = {&C};
+      void* args[] = {&C, &fl};
       if (cudaLaunchCooperativeKernel((const void*)c_stage, dim3(gs), dim3(256), args, 0, s) == cudaSuccess) return 1;
       cudaGetLastError();
       stage_blocks = 0;  // not available here: the separate kernels from now on
     }
     int gv = std::max(1, (nv + 255) / 256);
-    c_check<<<gv, 256, 0, s>>>(C);
+    c_check<<<gv, 256, 0, s>>>(C, fl);
     int n = enqueue_rebuild(s);
     c_contact<<<grid_pairs, 256, 0, s>>>(C);
     return 2 + n;

@@ -95,6 +95,19 @@ __device__ __forceinline__ float step_dt(const View& S, bool recommend, float dt
   return 1.0f / (6.283185f * sqrtf(mx));
 }
 
+// The collision stale vote (CVoxelyze::updateCollisions, src/Voxelyze.cpp:686-694) for the next
+// step, from this step's new positions: one warp ballot, one store per warp that saw a surface
+// voxel move past the rebuild distance.  Lanes past the scene's end vote false.
+__device__ __forceinline__ void col_vote(const View& S, bool moved) {
+  const unsigned any = __ballot_sync(0xffffffffu, moved);
+  if (any && (threadIdx.x & 31) == __ffs(any) - 1) *S.colVote = 1;
+}
+__device__ __forceinline__ bool col_moved(const View& S, int v, double px, double py, double pz) {
+  const int nv = S.nv;
+  const double dx = px - S.colLast[v], dy = py - S.colLast[nv + v], dz = pz - S.colLast[2 * nv + v];
+  return dx * dx + dy * dy + dz * dz > S.colRecalc2;
+}
+
 template <bool RECOMMEND, int DEC = 0>
 __global__ void __launch_bounds__(512) k_voxel(View S, float dt_fixed, int parity, float fallback,
                                                uint8_t* dec = nullptr) {
@@ -111,8 +124,14 @@ __global__ void __launch_bounds__(512) k_voxel(View S, float dt_fixed, int parit
     S.ctl->last_dt = dt;
     if (RECOMMEND) S.ctl->maxf[parity ^ 1] = 0u;  // next step's slot; nobody reads it in this pass
   }
-  if (v >= S.nv) return;
-  vx64::voxel_update<DEC>(S, v, dt, DEC ? dec + v : nullptr);
+  const bool live = v < S.nv;
+  if (live) vx64::voxel_update<DEC>(S, v, dt, DEC ? dec + v : nullptr);
+  if (S.colVote) {  // uniform for the launch
+    bool moved = false;
+    if (live && !(S.vflags[v] & VXG_VF_INTERIOR))
+      moved = col_moved(S, v, S.pos[v], S.pos[S.nv + v], S.pos[2 * S.nv + v]);
+    col_vote(S, moved);
+  }
 }
 
 // setAmbientTemperature(t, true): every voxel's temperature, then every link's rest length
@@ -635,8 +654,22 @@ __global__ void __launch_bounds__(512) k_voxel32(vx32::View S, float dt_fixed, i
     S.B.ctl->last_dt = dt;  // the next step's link pass reads it as every voxel's previous dt
     if (RECOMMEND) S.B.ctl->maxf[parity ^ 1] = 0u;
   }
-  if (!live) return;
-  vx32::voxel_step<FUSE_POIS>(S, v, dt, in);
+  if (!S.B.colVote) {  // uniform for the launch
+    if (live) vx32::voxel_step<FUSE_POIS>(S, v, dt, in);
+    return;
+  }
+  bool moved = false;
+  if (live) {
+    vx32::f3 d, c;
+    vx32::voxel_step<FUSE_POIS>(S, v, dt, in, &d, &c);
+    if (!(in.flags & VXG_VF_INTERIOR)) {  // the position as a host read converts it
+      const int nv = S.B.nv;
+      const double s = S.B.colS;
+      moved = col_moved(S.B, v, S.B.vidx[v] * s + ((double)d.x - (double)c.x),
+                        S.B.vidx[nv + v] * s + ((double)d.y - (double)c.y), in.iz * s + ((double)d.z - (double)c.z));
+    }
+  }
+  col_vote(S.B, moved);
 }
 // FP64 interchange fields <-> FP32C working state, one field per launch (only the fields the host
 // writes are converted on upload, only the fields it reads on download)
@@ -877,8 +910,10 @@ struct vxg_engine {
   int lp_bps = 0;
   int lp_fit[2] = {0, 0};
   // FP32C at a fixed dt with the one-thread-per-link kernels: the small-angle pass plus the general
-  // pass over the links it deferred (1, the default), or the general pass over every link (0)
-  int link_split = 1;
+  // pass over the links it deferred (1), or the general pass over every link (0, the default: the
+  // small-angle kernel needs as many registers as the general one, and the second launch made the
+  // step slower, 0.150 against 0.144 ms on the 128x128x64 lattice)
+  int link_split = 0;
   int lL_grid = 0;  // grid of the general pass over deferred links (resident blocks on every SM)
   int n_sm = 0;
   bool tab_poisson = false;  // some voxel material has nu != 0
@@ -1581,6 +1616,13 @@ inline void launch_pdl(bool pdl, void (*kernel)(KArgs...), int grid, int block, 
 
 static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEvent_t* ev = nullptr) {
   const View& S = e->S;
+  // the voxel pass's View: with collisions on it votes on the next step's stale test
+  View Sv = S;
+  vx32::View Vv = e->V;
+  if (e->g.collisions && e->col.ready()) {
+    e->col.voted(Sv, e->g);
+    Vv.B = Sv;
+  }
   bool rec = dt < 0;
   const int bl = e->blk_link, bv = e->blk_voxel;
   const int gl = grid_of(e->nl, bl), gv = grid_of(e->nv, bv);
@@ -1638,16 +1680,16 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
       }
     }
     if (ev) pass_event(ev[1], e->stream);
-    if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream);
+    if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream, first);
     if (ev) pass_event(ev[2], e->stream);
     e->n_launch += nk;
     const bool voxel_pdl = pdl_base && e->nl && e->lp_bps == 0 && !e->g.collisions;
     if (fused_poisson(e)) {
-      if (rec) k_voxel32<true, true><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
-      else launch_pdl(voxel_pdl, k_voxel32<false, true>, gv, bv, e->stream, e->V, dt, parity, e->g.fallback_freq2);
+      if (rec) k_voxel32<true, true><<<gv, bv, 0, e->stream>>>(Vv, dt, parity, e->g.fallback_freq2);
+      else launch_pdl(voxel_pdl, k_voxel32<false, true>, gv, bv, e->stream, Vv, dt, parity, e->g.fallback_freq2);
     } else {
-      if (rec) k_voxel32<true, false><<<gv, bv, 0, e->stream>>>(e->V, dt, parity, e->g.fallback_freq2);
-      else launch_pdl(voxel_pdl, k_voxel32<false, false>, gv, bv, e->stream, e->V, dt, parity, e->g.fallback_freq2);
+      if (rec) k_voxel32<true, false><<<gv, bv, 0, e->stream>>>(Vv, dt, parity, e->g.fallback_freq2);
+      else launch_pdl(voxel_pdl, k_voxel32<false, false>, gv, bv, e->stream, Vv, dt, parity, e->g.fallback_freq2);
     }
     if (ev) pass_event(ev[3], e->stream);
     return;
@@ -1657,22 +1699,22 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
     else k_link<false, true><<<gl, bl, 0, e->stream>>>(S, parity);
   }
   if (ev) pass_event(ev[1], e->stream);
-  if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream);
+  if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream, first);
   if (ev) pass_event(ev[2], e->stream);
   e->n_launch += nk;
   if (e->dec_mode) {  // one row of branch decisions per step (vxg_step checked the capacity)
     uint8_t* row = e->d_dec + (size_t)e->dec_step++ * (size_t)e->nv;
     if (e->dec_mode == 1) {
-      if (rec) k_voxel<true, 1><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2, row);
-      else k_voxel<false, 1><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2, row);
+      if (rec) k_voxel<true, 1><<<gv, bv, 0, e->stream>>>(Sv, dt, parity, e->g.fallback_freq2, row);
+      else k_voxel<false, 1><<<gv, bv, 0, e->stream>>>(Sv, dt, parity, e->g.fallback_freq2, row);
     } else {
-      if (rec) k_voxel<true, 2><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2, row);
-      else k_voxel<false, 2><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2, row);
+      if (rec) k_voxel<true, 2><<<gv, bv, 0, e->stream>>>(Sv, dt, parity, e->g.fallback_freq2, row);
+      else k_voxel<false, 2><<<gv, bv, 0, e->stream>>>(Sv, dt, parity, e->g.fallback_freq2, row);
     }
   } else if (rec) {
-    k_voxel<true><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+    k_voxel<true><<<gv, bv, 0, e->stream>>>(Sv, dt, parity, e->g.fallback_freq2);
   } else {
-    k_voxel<false><<<gv, bv, 0, e->stream>>>(S, dt, parity, e->g.fallback_freq2);
+    k_voxel<false><<<gv, bv, 0, e->stream>>>(Sv, dt, parity, e->g.fallback_freq2);
   }
   if (ev) pass_event(ev[3], e->stream);
 }
@@ -1752,6 +1794,7 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
       if (!e->bev[k]) VXG_CK(cudaEventCreate(&e->bev[k]));
     VXG_CK(cudaEventRecord(e->bev[0], e->stream));
   }
+  if (e->g.collisions) e->n_launch += e->col.enqueue_surface(e->stream);  // the batch's surface list
   e->tev_used = 0;
   if (use_graph) {
     if (nsteps >= chunk) {

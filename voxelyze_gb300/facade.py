@@ -468,7 +468,7 @@ class Engine:
 
     def set_link_split(self, on: bool):
         """FP32C link pass at a fixed dt: the small-angle kernel plus the general kernel over the
-        links it defers (default), or the general kernel over every link; identical results."""
+        links it defers, or the general kernel over every link (default); identical results."""
         self._ck(self.f["set_link_split"](self.sim.h, 1 if on else 0))
 
     def link_split(self) -> bool:
