@@ -5,8 +5,9 @@
   one material per voxel, per-voxel actuation phase, floor, friction, gravity; made by
   tests/golden/make_adjoint_ref_fd.py).  The GPU adjoint of the same run (FP64 path) is compared
   with their Richardson extrapolation for every parameter whose two differences (steps h and h/4)
-  agree within 10 %; where they do not, a friction or contact decision flipped between the
-  perturbed runs and the difference crosses a branch the adjoint does not follow.
+  agree within 1 %; where they do not, a floor-contact or static-friction decision somewhere in the
+  body flipped between the perturbed runs (the reference cannot replay a run's decisions), and the
+  difference measures that jump, not the derivative along the branches the adjoint follows.
 * voxelyze_gb300.autograd.AdjointComX: J.backward() returns the adjoint's gradient, and
   torch.autograd.gradcheck (central differences in float64 through the same Function) agrees
   with it on E, density and phase multipliers of a few voxels.
@@ -49,7 +50,7 @@ def test_adjoint_against_reference_differences(product_lib):
     rows = []
     for v, kind, (d1, d2, rich) in zip(fx["pick_voxel"], fx["pick_kind"], fx["fd"]):
         ad = grads[str(kind)][int(v)]
-        smooth = abs(d1 - d2) <= 0.1 * max(abs(d1), abs(d2))
+        smooth = abs(d1 - d2) <= 0.01 * max(abs(d1), abs(d2))
         rows.append((int(v), str(kind), ad, rich, abs(ad - rich) / abs(rich), smooth))
     for r in rows:
         print("voxel %4d %-5s adjoint % .6e  reference FD (Richardson) % .6e  rel. diff %.2e %s"
@@ -57,7 +58,7 @@ def test_adjoint_against_reference_differences(product_lib):
     print(f"objective: GPU {obj[0]:.15e}, reference {float(fx['objective']):.15e} (rel. {rel_obj:.2e})")
     assert rel_obj <= 1e-9
     smooth = [r for r in rows if r[5]]
-    assert len(smooth) >= 8
+    assert len(smooth) >= 10 and {r[1] for r in smooth} == {"E", "rho", "phase"}
     assert max(r[4] for r in smooth) <= 2e-3
 
 
