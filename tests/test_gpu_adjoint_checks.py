@@ -10,7 +10,9 @@
   difference measures that jump, not the derivative along the branches the adjoint follows.
 * voxelyze_gb300.autograd.AdjointComX: J.backward() returns the adjoint's gradient, and
   torch.autograd.gradcheck (central differences in float64 through the same Function) agrees
-  with it on E, density and phase multipliers of a few voxels.
+  with it on E, density and phase multipliers of a few voxels; the Function evaluates J with the
+  unperturbed run's floor-contact and static-friction decisions replayed, so the differences
+  follow the branches the adjoint differentiates along.
 """
 from __future__ import annotations
 
@@ -67,7 +69,7 @@ def test_autograd_function(product_lib):
     from voxelyze_gb300.autograd import AdjointComX, ComXObjective
 
     sc = S.graded_population(n_bodies=2, side=5, occupancy=0.7, seed=33)
-    objective = ComXObjective(product_lib, sc, nsteps=300, checkpoint_every=50)
+    objective = ComXObjective(product_lib, sc, nsteps=300, checkpoint_every=50, freeze_decisions=True)
     E0, R0, P0 = (torch.tensor(a, dtype=torch.float64) for a in objective.initial())
     E, R, P = (t.clone().requires_grad_(True) for t in (E0, R0, P0))
     J = AdjointComX.apply(E, R, P, objective)

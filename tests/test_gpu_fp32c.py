@@ -85,6 +85,42 @@ def test_population_with_temperature(product_lib, friction):
         assert rel_disp <= 1e-3
 
 
+def test_friction_error_is_the_scene_conditioning(product_lib):
+    """The friction population's FP32C error is the conditioning of the scene, not of FP32C: two
+    FP64 runs whose only difference is one ulp in every initial voxel position (nextafter towards
+    +inf) drift apart by an amount of the same order as FP32C drifts from FP64 over the same 500
+    steps.  The static-friction latch compares the horizontal force with mu * N while N is ~0 at
+    first contact (src/VX_Voxel.cpp:285-291), so any rounding difference can flip it for a voxel,
+    which then slides."""
+    import ctypes as C
+
+    sc = S.population(16, 4, 10)
+    a, b = _pair(product_lib, sc)
+    c = make_sim(product_lib, "vx", sc)
+    product_lib.vx_engine.restype = C.c_void_p
+    product_lib.vx_engine.argtypes = [C.c_void_p]
+    product_lib.vxg_set_field.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong]
+    pos = c.voxel_state()["pos"]
+    bumped = np.ascontiguousarray(np.nextafter(pos, np.inf).T).ravel()  # component-major
+    VXG_F_POS = 4
+    assert product_lib.vxg_set_field(product_lib.vx_engine(C.c_void_p(c.h)), VXG_F_POS, bumped.ctypes.data,
+                                     bumped.size) == 0
+    dt = a.recommended_time_step()
+    for s in (b, c):
+        s.recommended_time_step()
+    for k in range(10):
+        t = float(0.1 * np.sin(2 * np.pi * 2 * k * 50 * dt))
+        for s in (a, b, c):
+            s.set_ambient_temperature(t, True)
+            assert s.do_time_steps(50, dt) == 50
+    _, d32 = _errors(a, b, sc)
+    _, d64 = _errors(a, c, sc)
+    print(f"population 16 bodies with friction, 500 steps: FP32C vs FP64 {d32:.3e}, FP64 with one ulp "
+          f"moved in every initial position vs FP64 {d64:.3e} (relative to the largest displacement)")
+    assert d64 > 0.0
+    assert d64 >= 0.1 * d32
+
+
 def test_cantilever_small_deflection(product_lib):
     """Static-like cantilever (small load): FP32C converges to the same deflection."""
     sc = S.cantilever(20, 4, 4, voxel_size=0.005, tip_force=-0.01)

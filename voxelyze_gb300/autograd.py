@@ -28,7 +28,7 @@ class ComXObjective:
     multi-body scene whose per-voxel parameters are the inputs."""
 
     def __init__(self, lib, scene, nsteps: int, checkpoint_every: int = 100, amplitude: float = 0.1,
-                 frequency: float = 2.0, dt: float | None = None):
+                 frequency: float = 2.0, dt: float | None = None, freeze_decisions: bool = False):
         if scene.body is None or len(scene.materials) != scene.n_voxels:
             raise ValueError("needs a multi-body scene with one material per voxel")
         self.lib, self.scene = lib, scene
@@ -39,6 +39,17 @@ class ComXObjective:
             sim, _ = self._build(*self.initial())
             dt = sim.recommended_time_step()
         self.dt = float(dt)
+        # freeze_decisions: J is evaluated with the floor-contact and static-friction decisions of
+        # the run at the scene's own parameters replayed (vxg_set_decisions), so that values at
+        # perturbed parameters follow the branches the adjoint differentiates along
+        self.decisions = None
+        if freeze_decisions:
+            sim, eng = self._build(*self.initial())
+            sim.recommended_time_step()
+            eng.set_decisions(1, nsteps)
+            if sim.do_time_steps(nsteps, self.dt) != nsteps:
+                raise RuntimeError("the run diverged")
+            self.decisions = eng.decisions(nsteps)
 
     def initial(self):
         """The scene's own (E, rho, phase) as float64 arrays."""
@@ -63,7 +74,16 @@ class ComXObjective:
         sim, eng = self._build(E, rho, phase)
         sim.recommended_time_step()  # the reference's first call also refreshes link state
         obj, gE, gR, gP = eng.adjoint_com_x(self.nsteps, self.dt, self.offsets, checkpoint_every=self.checkpoint_every)
-        return float(obj.sum()), gE, gR, gP
+        J = float(obj.sum())
+        if self.decisions is not None:  # the value along the recorded branches
+            sim, eng = self._build(E, rho, phase)
+            sim.recommended_time_step()
+            eng.set_decisions(2, self.nsteps)
+            eng.put_decisions(self.decisions)
+            if sim.do_time_steps(self.nsteps, self.dt) != self.nsteps:
+                raise RuntimeError("the run diverged")
+            J = float(eng.body_com(self.offsets)[:, 0].sum())
+        return J, gE, gR, gP
 
 
 class AdjointComX(torch.autograd.Function):

@@ -263,11 +263,14 @@ VX_HD void link_gather_own(const View& S, int l, LinkIn& in, int& vn, int& vp) {
   vn = B.lvox[l];
   vp = B.lvox[nl + l];
 }
-template <bool POIS>
+// ACT: the voxels' temperatures were set for this step (in-step actuation): the rest length offset
+// is recomputed from them here, as CVX_Link::updateRestLength does after setTemperature
+// (src/VX_Link.cpp:137-140), instead of in a separate pass; the caller stores it.
+template <bool POIS, bool ACT = false>
 VX_HD void link_gather_ends(const View& S, int l, LinkIn& in, int vn, int vp) {
   const vx64::View& B = S.B;
   const int nv = B.nv;
-  in.rd = S.restDelta[l];
+  in.rd = ACT ? rest_delta(S, vn, vp, (in.lf >> 8) & 3) : S.restDelta[l];
   in.dn = f3_of(S.P[vn]);
   in.dp = f3_of(S.P[vp]);
   in.qn = q4_of(S.Q[vn]);
@@ -281,25 +284,25 @@ VX_HD void link_gather_ends(const View& S, int l, LinkIn& in, int vn, int vp) {
     in.psn = in.psp = F3(0, 0, 0);
   }
 }
-template <bool POIS>
+template <bool POIS, bool ACT = false>
 VX_HD LinkIn link_gather(const View& S, int l) {
   LinkIn in;
   int vn, vp;
   link_gather_own<POIS>(S, l, in, vn, vp);
-  link_gather_ends<POIS>(S, l, in, vn, vp);
+  link_gather_ends<POIS, ACT>(S, l, in, vn, vp);
   return in;
 }
 
 // CVX_Link::updateForces + orientLink + updateStrain in FP32C for link l from its gathered inputs;
 // writes the link's new state and returns the axial strain (the divergence test's value).
-// pdt is every voxel's previous time step (the local damping divides by it).
+// ipdt is the reciprocal of every voxel's previous time step (the local damping divides by it).
 // SMALL: the caller has seen the small-angle flag set.  The link's angle1 is then the identity and
 // its rotation vector zero for the whole step, unless the hysteresis test below moves it to the
 // large-angle branch: in that case nothing is written, *deferred is set, and the general form
 // (SMALL = false) must process the link from the same inputs.  For a link that stays small-angle
 // both forms evaluate the same expressions in the same order, so their results are bit-identical.
 template <bool SMALL>
-VX_HDN float link_compute_t(const View& S, int l, const LinkIn& in, float pdt, bool* deferred) {
+VX_HDN float link_compute_t(const View& S, int l, const LinkIn& in, float ipdt, bool* deferred) {
   const vx64::View& B = S.B;
   const int nl = B.nl;
   uint32_t lf = in.lf;
@@ -325,19 +328,30 @@ VX_HDN float link_compute_t(const View& S, int l, const LinkIn& in, float pdt, b
   q4 angle2 = qmul(tr, a2);
   q4 angle1 = Q4(1, 0, 0, 0);
   float px = s + ex;
-  float smallTurn = (fabsf(pz) + fabsf(py)) / px;
   const float iL = 1.0f / L;  // one division for the two uses of the current length
   float extendPerc = fabsf((ex - rd) * iL);
   const float HF = 1.2f, BEND = 0.05f, EXT = 0.50f;
+  // the bend (|pz| + |py|) / px against its two thresholds, compared as products where px > 0
+  // (every link short of folding over); the quotient itself otherwise
+  const float turn = fabsf(pz) + fabsf(py);
+  bool bentBelow, bentAbove;
+  if (px > 0.0f) {
+    bentBelow = turn < BEND * px;
+    bentAbove = turn > (HF * BEND) * px;
+  } else {
+    const float smallTurn = turn / px;
+    bentBelow = smallTurn < BEND;
+    bentAbove = smallTurn > HF * BEND;
+  }
   if (SMALL) {
-    if (smallTurn > HF * BEND || extendPerc > HF * EXT) {
+    if (bentAbove || extendPerc > HF * EXT) {
       *deferred = true;
       return 0.0f;
     }
-  } else if (!smallAngle && smallTurn < BEND && extendPerc < EXT) {
+  } else if (!smallAngle && bentBelow && extendPerc < EXT) {
     smallAngle = true;
     lvv = false;
-  } else if (smallAngle && (smallTurn > HF * BEND || extendPerc > HF * EXT)) {
+  } else if (smallAngle && (bentAbove || extendPerc > HF * EXT)) {
     smallAngle = false;
     lvv = false;
   }
@@ -401,7 +415,6 @@ VX_HDN float link_compute_t(const View& S, int l, const LinkIn& in, float pdt, b
     mP = F3(a2c * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z));
     if (lvv) {
       f3 pc = F3(m.sqA1 * dPos2.x, m.sqB1 * dPos2.y - m.sqB2xFMp * (dA1.z + dA2.z), m.sqB1 * dPos2.z + m.sqB2xFMp * (dA1.y + dA2.y));
-      const float ipdt = 1.0f / pdt;
       float dmN = 2 * mn.sqrtMass * mn.zetaInternal * ipdt, dmP = 2 * mp.sqrtMass * mp.zetaInternal * ipdt;
       fN.x += dmN * pc.x; fN.y += dmN * pc.y; fN.z += dmN * pc.z;
       fP.x -= dmP * pc.x; fP.y -= dmP * pc.y; fP.z -= dmP * pc.z;
@@ -434,13 +447,15 @@ VX_HDN float link_compute_t(const View& S, int l, const LinkIn& in, float pdt, b
   if (nf != lf) B.lflags[l] = nf;
   return axial;
 }
-VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float pdt) {
-  return link_compute_t<false>(S, l, in, pdt, nullptr);
+VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float ipdt) {
+  return link_compute_t<false>(S, l, in, ipdt, nullptr);
 }
 
-template <bool POIS>
+template <bool POIS, bool ACT = false>
 VX_HDN float link_update(const View& S, int l) {
-  return link_compute(S, l, link_gather<POIS>(S, l), S.B.ctl->last_dt);  // every voxel stepped with last_dt
+  const LinkIn in = link_gather<POIS, ACT>(S, l);
+  if (ACT) S.restDelta[l] = in.rd;
+  return link_compute(S, l, in, S.B.ctl->inv_last_dt);  // every voxel stepped with last_dt
 }
 
 // The small-angle form for link l whose flags lf the caller has read and found small-angle:
@@ -466,7 +481,7 @@ VX_HDN float link_update_small(const View& S, int l, uint32_t lf, bool* deferred
   in.strainOffset = B.strainOffset[l];
   const int vn = B.lvox[l], vp = B.lvox[nl + l];
   link_gather_ends<POIS>(S, l, in, vn, vp);
-  return link_compute_t<true>(S, l, in, B.ctl->last_dt, deferred);
+  return link_compute_t<true>(S, l, in, B.ctl->inv_last_dt, deferred);
 }
 
 

@@ -59,6 +59,8 @@ struct Ctl {
   int pad_;
   float time;           // CVoxelyze::currentTime
   float last_dt;
+  float inv_last_dt;    // 1 / last_dt (IEEE division), for the FP32C link pass's local damping
+  int pad2_;
   unsigned long long counters[VXG_C_COUNT];
 };
 

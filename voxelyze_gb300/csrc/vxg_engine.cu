@@ -122,6 +122,7 @@ __global__ void __launch_bounds__(512) k_voxel(View S, float dt_fixed, int parit
     S.ctl->steps += 1;
     S.ctl->time += dt;
     S.ctl->last_dt = dt;
+    S.ctl->inv_last_dt = 1.0f / dt;
     if (RECOMMEND) S.ctl->maxf[parity ^ 1] = 0u;  // next step's slot; nobody reads it in this pass
   }
   const bool live = v < S.nv;
@@ -430,7 +431,9 @@ int grid_of(int n, int b) { return std::max(1, (n + b - 1) / b); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
-template <bool RECOMMEND, bool FORCES, bool POIS>
+// ACT: in-step actuation set the temperatures just before: the rest length offsets are recomputed
+// here from them (no separate rest-length pass)
+template <bool RECOMMEND, bool FORCES, bool POIS, bool ACT = false>
 __global__ void __launch_bounds__(512) k_link32(vx32::View S, int parity) {
   int l = blockIdx.x * blockDim.x + threadIdx.x;
   // nothing is read before the wait (loading the link's own state ahead of it measured slower)
@@ -446,7 +449,7 @@ __global__ void __launch_bounds__(512) k_link32(vx32::View S, int parity) {
   }
   if (RECOMMEND) block_max_to(&S.B.ctl->maxf[parity], f2);
   if (!FORCES || !live) return;
-  if (vx32::link_update<POIS>(S, l) > 100) S.B.ctl->diverged = 1;
+  if (vx32::link_update<POIS, ACT>(S, l) > 100) S.B.ctl->diverged = 1;
 }
 
 // ---- split FP32C link pass ----------------------------------------------------------------------
@@ -596,7 +599,7 @@ __global__ void __launch_bounds__(kLpT) k_link32p(vx32::View S, int ntiles) {
   const vx64::View& B = S.B;
   if (B.ctl->halt) return;
   const int t = threadIdx.x, nl = B.nl, G = gridDim.x;
-  const float pdt = B.ctl->last_dt;  // every voxel stepped with the same dt last step
+  const float ipdt = B.ctl->inv_last_dt;  // every voxel stepped with the same dt last step
   int tile = blockIdx.x;
   if (tile >= ntiles) return;
   // prologue: ids of the first two tiles, copies of the first
@@ -621,7 +624,7 @@ __global__ void __launch_bounds__(kLpT) k_link32p(vx32::View S, int ntiles) {
     cp_async_commit();
     cp_async_wait1();  // this tile's copies (all but the group just committed) have landed
     l = tile * kLpT + t;
-    if (l < nl) diverged |= vx32::link_compute(S, l, lp_read<POIS>(cur, t), pdt) > 100;
+    if (l < nl) diverged |= vx32::link_compute(S, l, lp_read<POIS>(cur, t), ipdt) > 100;
     tile = nt;
     nt = t2;
     l1 = l2;
@@ -652,6 +655,7 @@ __global__ void __launch_bounds__(512) k_voxel32(vx32::View S, float dt_fixed, i
     S.B.ctl->steps += 1;
     S.B.ctl->time += dt;
     S.B.ctl->last_dt = dt;  // the next step's link pass reads it as every voxel's previous dt
+    S.B.ctl->inv_last_dt = 1.0f / dt;
     if (RECOMMEND) S.B.ctl->maxf[parity ^ 1] = 0u;
   }
   if (!S.B.colVote) {  // uniform for the launch
@@ -715,7 +719,12 @@ __global__ void k_conv(vx32::View S, double s, int field, int to32) {
       break;
     case VXG_F_ANGMOM: cv(B.angMom, S.ang, 3, nv); break;
     case VXG_F_PREV_DT:
-      if (to32) { if (i == 0 && nv) B.ctl->last_dt = B.prevDt[0]; }
+      if (to32) {
+        if (i == 0 && nv) {
+          B.ctl->last_dt = B.prevDt[0];
+          B.ctl->inv_last_dt = 1.0f / B.prevDt[0];
+        }
+      }
       else if (i < nv) B.prevDt[i] = B.ctl->last_dt;
       break;
     case VXG_F_POS2: cv(B.pos2, S.pos2, 3, nl); break;
@@ -754,14 +763,21 @@ __global__ void k_pos_out(vx32::View S, double s, double* dst) {
 // (src/Voxelyze.cpp:585-594, src/VX_Voxel.cpp:108-114).  Evaluated in double with the correctly
 // rounded sine on the FP64 path, in float on the FP32C path; the result is rounded to float like
 // the reference's float temperature argument.
-__global__ void k_actuate(View S, double amp, double freq, const float* phase, int fp32) {
+// The actuation temperature amp * sin(2 pi freq t + phase[v]) of every voxel at the step's start
+// time t.  FP64: the argument and the sine in double, rounded once to the float temperature as the
+// reference's driver would compute it.  FP32C (fp32 != 0): in float (w32 = 2 pi freq and amp32 as
+// floats), which keeps the FP64 pipe out of the pass.  Launched to overlap the previous voxel
+// pass's tail where that pass is the kernel before it: nothing is read before the wait.
+__global__ void k_actuate(View S, double amp, double freq, const float* phase, int fp32, float amp32, float w32) {
+  pdl_wait();
+  pdl_trigger();
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= S.nv || S.ctl->halt) return;
-  double arg = 2.0 * 3.141592653589793 * freq * (double)S.ctl->time + (phase ? (double)phase[v] : 0.0);
   float t;
   if (fp32) {
-    t = (float)amp * sinf((float)arg);
+    t = amp32 * sinf(w32 * S.ctl->time + (phase ? phase[v] : 0.0f));
   } else {
+    const double arg = 2.0 * 3.141592653589793 * freq * (double)S.ctl->time + (phase ? (double)phase[v] : 0.0);
     // Ziv's rounding test: only the float result is kept.  The library sine is within a few ulp of
     // sin(arg), so amp * sin(arg) lies within 2^-45 (relative) of y; when that whole interval
     // rounds to one float, it is the float the correctly rounded sine gives.  Otherwise (about one
@@ -1635,13 +1651,21 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   // collision stage), a first step (conversions may precede it) or timing events make the launch
   // an ordinary one.
   const bool pdl_base = e->pdl && !ev && e->precision == VXG_FP32C;
-  bool link_pdl = pdl_base && !first && !e->act_mode;
-  long long nk = 1 + (e->nl ? 1 : 0) + (e->act_mode && e->nv ? 1 + (e->nl ? 1 : 0) : 0) +
+  // FP32C at a fixed dt with the default link pass: the actuation's rest-length update happens in
+  // the link pass itself (k_link32<..., ACT>), which directly follows the actuation kernel
+  const bool act_fused = e->act_mode && e->nv && e->nl && e->precision == VXG_FP32C && !rec && e->lp_bps == 0 &&
+                         !e->link_split && !(e->g.any_poisson && !fused_poisson(e));
+  bool link_pdl = pdl_base && !first && (!e->act_mode || act_fused);
+  long long nk = 1 + (e->nl ? 1 : 0) + (e->act_mode && e->nv ? 1 + (e->nl && !act_fused ? 1 : 0) : 0) +
                  (e->g.any_poisson && e->nv && !fused_poisson(e) ? 1 : 0);
   if (e->act_mode && e->nv) {
-    k_actuate<<<grid_for(e->nv), kBlock, 0, e->stream>>>(S, e->act_amp, e->act_freq, e->act_mode == 2 ? e->d_phase : nullptr,
-                                                        e->precision == VXG_FP32C ? 1 : 0);
-    if (e->nl) {
+    const float* ph = e->act_mode == 2 ? e->d_phase : nullptr;
+    const int fp32 = e->precision == VXG_FP32C ? 1 : 0;
+    const float amp32 = (float)e->act_amp, w32 = (float)(2.0 * 3.141592653589793 * e->act_freq);
+    // right after the previous step's voxel pass (not the first step of a batch): may overlap its tail
+    launch_pdl(pdl_base && !first, k_actuate, grid_for(e->nv), kBlock, e->stream, S, e->act_amp, e->act_freq, ph, fp32,
+               amp32, w32);
+    if (e->nl && !act_fused) {
       if (e->precision == VXG_FP32C) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
       else k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(S);
     }
@@ -1674,6 +1698,9 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
           launch_pdl(pdl_base, k_link32L<false>, gL, 256, e->stream, e->V);
         }
         nk += 1;
+      } else if (act_fused) {
+        if (pois) launch_pdl(link_pdl, k_link32<false, true, true, true>, gl, bl, e->stream, e->V, parity);
+        else launch_pdl(link_pdl, k_link32<false, true, false, true>, gl, bl, e->stream, e->V, parity);
       } else {
         if (pois) launch_pdl(link_pdl, k_link32<false, true, true>, gl, bl, e->stream, e->V, parity);
         else launch_pdl(link_pdl, k_link32<false, true, false>, gl, bl, e->stream, e->V, parity);
