@@ -318,6 +318,17 @@ def run_ours(args, world, rank, local):
     nv, nl = sim64.voxel_count(), sim64.link_count()
     dt = sim64.recommended_time_step()
     sim32.recommended_time_step()
+    # launch shapes, link-pass variant and graph length from the engine's autotuner (it restores the
+    # state it stepped); untimed
+    launch = {}
+    for name, sim in (("fp64", sim64), ("fp32c", sim32)):
+        E = F.Engine(sim)
+        if not args.no_autotune:
+            E.autotune(16, dt)
+        blk = E.launch()
+        launch[name] = {"block_link": blk[0], "block_voxel": blk[1], "graph_chunk": blk[2],
+                        "link_pipeline": E.link_pipeline(), "link_split": E.link_split(),
+                        "autotuned": not args.no_autotune}
     for sim in (sim64, sim32):
         if sim.do_time_steps(args.warmup, dt) != args.warmup:
             raise RuntimeError("warm-up diverged")
@@ -459,6 +470,7 @@ def run_ours(args, world, rank, local):
                                            "ms_per_step": o["total_ms"] / args.steps,
                                            "per_pass_ms": {"link": o["link_ms"], "collide": o["collide_ms"],
                                                            "voxel": o["voxel_ms"]}},
+                       "launch": launch,
                        "fp32c_over_fp64": (t_head["value"] / o["value"]) if fp32 else (o["value"] / t_head["value"]),
                        "fp32c_error_vs_fp64": err, **extra},
             "roofline": roof, "roofline_fp64": fp64_roof, "cpu_baseline": cpu,
@@ -564,6 +576,7 @@ def main():
     ap.add_argument("--precision", default="fp32c", choices=["fp64", "fp32c"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the engine's default launch shapes")
     ap.add_argument("--quick-error", action="store_true",
                     help="report the FP32C error where the timed steps end, not at the workload's horizon")
     ap.add_argument("--dims", default="128,128,64", help="lattice size (smaller cases for profiling)")

@@ -117,6 +117,7 @@ int vx_restore(void* s, int slot);                          /* vxg_restore (same
 int vx_adjoint_com_x(void* s, int nsteps, float dt, int checkpoint_every, const int* body_offsets, int n_bodies,
                      double* objective, double* dE, double* drho, double* dphase);
 int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk); /* vxg_set_launch */
+int vx_get_launch(void* s, int* block_link, int* block_voxel, int* graph_chunk); /* vxg_get_launch */
 int vx_autotune(void* s, int trial_steps, float dt, int* out3);            /* vxg_autotune: link, voxel, chunk */
 int vx_set_link_pipeline(void* s, int blocks_per_sm);                      /* vxg_set_link_pipeline */
 int vx_get_link_pipeline(void* s, int* blocks_per_sm);                     /* vxg_get_link_pipeline */

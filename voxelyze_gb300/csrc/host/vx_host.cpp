@@ -1583,6 +1583,11 @@ int vx_set_launch(void* s, int block_link, int block_voxel, int graph_chunk) {
   if (!vx.upload()) return -1;
   return vxg_set_launch(vx.impl()->eng, block_link, block_voxel, graph_chunk) ? -1 : 0;
 }
+int vx_get_launch(void* s, int* block_link, int* block_voxel, int* graph_chunk) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_get_launch(vx.impl()->eng, block_link, block_voxel, graph_chunk) ? -1 : 0;
+}
 int vx_set_link_pipeline(void* s, int blocks_per_sm) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.upload()) return -1;

@@ -1209,6 +1209,9 @@ int vxg_create(vxg_engine** out, int device, int precision) {
   vxg_engine* e = new vxg_engine();
   e->device = device;
   e->precision = precision;
+  // FP32C link pass: 128-thread blocks measured ~2 % faster than 256 on GB300 (vxg_autotune
+  // compares all shapes)
+  if (precision == VXG_FP32C) e->blk_link = 128;
   cudaError_t c = cudaSetDevice(device);
   if (c != cudaSuccess) { delete e; return VXG_E_CUDA; }
   c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);

@@ -406,6 +406,7 @@ _EXT_SIGS = {
     "restore": (_i, [_p, _i]),
     "set_launch": (_i, [_p, _i, _i, _i]),
     "autotune": (_i, [_p, _i, _f, _ip]),
+    "get_launch": (_i, [_p, _ip, _ip, _ip]),
     "set_link_pipeline": (_i, [_p, _i]),
     "get_link_pipeline": (_i, [_p, _ip]),
     "set_link_split": (_i, [_p, _i]),
@@ -499,6 +500,13 @@ class Engine:
         out = np.zeros(1, np.int32)
         self._ck(self.f["get_link_pipeline"](self.sim.h, _ptr(out, C.c_int)))
         return int(out[0])
+
+    def launch(self) -> tuple:
+        """(threads per block of the link pass, of the voxel pass, steps per captured graph)."""
+        out = np.zeros(3, np.int32)
+        self._ck(self.f["get_launch"](self.sim.h, _ptr(out[0:], C.c_int), _ptr(out[1:], C.c_int),
+                                      _ptr(out[2:], C.c_int)))
+        return tuple(int(x) for x in out)
 
     def autotune(self, trial_steps: int = 20, dt: float = -1.0) -> tuple:
         out = np.zeros(3, np.int32)
