@@ -15,13 +15,16 @@
 //              c_insert  surface voxels into a uniform hash grid (cell = watch radius), open
 //                        addressing on the packed cell key, one linked list per cell
 //              c_count   each surface voxel counts partners within the watch radius that are not
-//                        lattice neighbours (the 5-hop list, binary search) - all, and those after it
+//                        lattice neighbours (the 5-hop list, binary search) - all, and those after
+//                        it; one warp per voxel, lane k walking the k-th of the 27 cells around it
 //              c_scan    exclusive scans give each voxel its slot in the pair list and in the
 //                        contact list
-//              c_fill    each voxel sorts its partners; pairs (i, j > i) land in the reference's
-//                        list order (i ascending, then j ascending)
+//              c_fill    each voxel's partners, packed by the lanes into the warp's shared buffer
+//                        and placed by rank; pairs (i, j > i) land in the reference's list order
+//                        (i ascending, then j ascending)
 //              c_watch   each voxel's contact list: partners ascending, with the pair index found
-//                        in the partner's sorted list (the order the reference's colWatch ends in)
+//                        in the partner's sorted list (the order the reference's colWatch ends in),
+//                        one lane per partner
 //   c_contact  one thread per pair: the penalty + damping contact force (float math)
 // The voxel pass subtracts each voxel's contact forces in its contact-list order.
 #pragma once
@@ -34,7 +37,8 @@ struct ColCtl {
   int nwatch;
   int status;       // overflow bits
   int rebuilds;
-  int vote;         // set by a voxel pass whose new positions make the pair list stale
+  int vote[2];      // set by a voxel pass whose new positions make the pair list stale; slot =
+                    // the step's parity (the stage of the next step reads it, and clears its own)
   int nsurf;        // surface voxels listed by c_surface
 };
 
@@ -69,6 +73,8 @@ struct ColView {
   int* cntGt;                // nv
   int* cntAll;               // nv
   int* surf;                 // nv: the surface voxels (c_surface), nsurf of them
+  double* spos;              // 3 nv: a surface voxel's position at the rebuild (cpos), set by c_insert
+  int* scell;                // 3 nv: its hash-grid cell coordinates, set by c_insert
   int* pairOff;              // nv + 1
   int* watchOff;             // nv + 1
   int* watchPartner;         // wcap
@@ -138,20 +144,21 @@ __global__ void c_surface(ColView C) {
   base = __shfl_sync(0xffffffffu, base, leader);
   if (surf) C.surf[base + __popc(m & ((1u << lane) - 1u))] = v;
 }
-// first step of a batch: the full stale test over the surface list; later steps: the voxel pass's
-// vote.  Either way the vote is cleared for the step's own voxel pass.
+// first step of a batch: the full stale test over the surface list; later steps: the vote the
+// previous step's voxel pass cast (slot parity ^ 1).  Either way this step's slot is cleared for
+// its own voxel pass.
 __device__ __forceinline__ bool c_moved_listed(const ColView& C, int first, int stride) {
   bool moved = false;
   const int n = C.cc->nsurf;
   for (int i = first; i < n; i += stride) moved |= c_moved(C, C.surf[i]);
   return moved;
 }
-__global__ void c_check(ColView C, int full) {
+__global__ void c_check(ColView C, int full, int parity) {
   if (C.ctl->halt || C.ctl->diverged) return;  // the same for the whole launch
   const int first = blockIdx.x * blockDim.x + threadIdx.x;
   if (first == 0) {
-    if (C.cc->force_stale || (!full && C.cc->vote)) C.cc->stale = 1;
-    C.cc->vote = 0;
+    if (C.cc->force_stale || (!full && C.cc->vote[parity ^ 1])) C.cc->stale = 1;
+    C.cc->vote[parity] = 0;
   }
   if (full && __syncthreads_or(c_moved_listed(C, first, gridDim.x * blockDim.x)) && threadIdx.x == 0) C.cc->stale = 1;
 }
@@ -172,19 +179,26 @@ __global__ void c_clear(ColView C) {
   c_clear_range(C, blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x, (unsigned long long)gridDim.x * blockDim.x);
 }
 
-__device__ __forceinline__ void cell_of(const ColView& C, int v, long long* c) {
-  c[0] = (long long)floor(cpos(C, v, 0) / C.cell);
-  c[1] = (long long)floor(cpos(C, v, 1) / C.cell);
-  c[2] = (long long)floor(cpos(C, v, 2) / C.cell);
-}
 
+// each surface voxel's position and cell, computed once per rebuild: the pair tests then read
+// them instead of rebuilding both positions (FP64 arithmetic, slow on GB300) for every candidate
 __device__ void c_insert_one(const ColView& C, int v) {
   if (v >= C.nv || !is_surface(C, v)) return;
-  C.lastWatch[v] = (float)cpos(C, v, 0);
-  C.lastWatch[C.nv + v] = (float)cpos(C, v, 1);
-  C.lastWatch[2 * C.nv + v] = (float)cpos(C, v, 2);
+  const int nv = C.nv;
+  const double p0 = cpos(C, v, 0), p1 = cpos(C, v, 1), p2 = cpos(C, v, 2);
+  C.lastWatch[v] = (float)p0;
+  C.lastWatch[nv + v] = (float)p1;
+  C.lastWatch[2 * nv + v] = (float)p2;
+  C.spos[v] = p0;
+  C.spos[nv + v] = p1;
+  C.spos[2 * nv + v] = p2;
   long long c[3];
-  cell_of(C, v, c);
+  c[0] = (long long)floor(p0 / C.cell);
+  c[1] = (long long)floor(p1 / C.cell);
+  c[2] = (long long)floor(p2 / C.cell);
+  C.scell[v] = (int)c[0];
+  C.scell[nv + v] = (int)c[1];
+  C.scell[2 * nv + v] = (int)c[2];
   unsigned long long k = cell_key(c[0], c[1], c[2]);
   unsigned long long h = hash64(k) & C.hcap_mask;
   for (unsigned long long probe = 0; probe <= C.hcap_mask; ++probe) {
@@ -226,36 +240,14 @@ __device__ __forceinline__ bool in_sorted(const int* a, int n, int x) {
 // is (v, u) a collision pair of regenerateCollisions (Voxelyze.cpp:735-745)?
 __device__ __forceinline__ bool is_pair(const ColView& C, int v, int u) {
   int i = v < u ? v : u, j = v < u ? u : v;
-  double dx = cpos(C, i, 0) - cpos(C, j, 0), dy = cpos(C, i, 1) - cpos(C, j, 1), dz = cpos(C, i, 2) - cpos(C, j, 2);
+  const int nv = C.nv;
+  double dx = C.spos[i] - C.spos[j], dy = C.spos[nv + i] - C.spos[nv + j], dz = C.spos[2 * nv + i] - C.spos[2 * nv + j];
   if (dx * dx + dy * dy + dz * dz > C.thr) return false;
   int b = C.nbOff[i], e = C.nbOff[i + 1];
   return !in_sorted(C.nbItem + b, e - b, j);
 }
 
-template <class F>
-__device__ __forceinline__ void for_partners(const ColView& C, int v, F&& f) {
-  long long c[3];
-  cell_of(C, v, c);
-  for (int dz = -1; dz <= 1; ++dz)
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        int u = find_cell(C, cell_key(c[0] + dx, c[1] + dy, c[2] + dz));
-        for (; u >= 0; u = C.next[u])
-          if (u != v && is_pair(C, v, u)) f(u);
-      }
-}
-
-__device__ void c_count_one(const ColView& C, int v) {
-  if (v >= C.nv) return;
-  int all = 0, gt = 0;
-  if (is_surface(C, v)) for_partners(C, v, [&](int u) { all++; gt += u > v; });
-  C.cntAll[v] = all;
-  C.cntGt[v] = gt;
-}
-__global__ void c_count(ColView C) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c_rebuilding(C) && i < C.cc->nsurf) c_count_one(C, C.surf[i]);
-}
+__global__ void c_count(ColView C);
 
 // exclusive scans of cntGt -> pairOff and cntAll -> watchOff by one block of up to 1024 threads
 // (rebuilds are rare)
@@ -296,31 +288,75 @@ __global__ void c_scan(ColView C) {
   if (c_rebuilding(C)) c_scan_block(C);
 }
 
-__device__ void c_fill_one(const ColView& C, int v) {
-  if (v >= C.nv || !is_surface(C, v)) return;
-  int buf[kMaxPartners];
-  int n = 0;
-  for_partners(C, v, [&](int u) {
-    if (n < kMaxPartners) buf[n] = u;
-    n++;
-  });
+__global__ void c_fill(ColView C);
+
+__global__ void c_watch(ColView C);
+
+// ---- warp-cooperative rebuild phases ------------------------------------------------------------
+// One warp per surface voxel v.  Lane k < 27 walks the list of the k-th cell around v's, so the 27
+// list walks and their pair tests (distance, then a binary search of the nearby list) run side by
+// side instead of one after another; lanes 27-31 only take part in the warp reductions.  Every
+// warp-collective call below is reached by all 32 lanes.
+template <class F>
+__device__ __forceinline__ void warp_partners(const ColView& C, int v, int lane, F&& f) {
+  if (lane >= 27) return;
+  const long long c[3] = {C.scell[v], C.scell[C.nv + v], C.scell[2 * C.nv + v]};
+  const int dz = lane / 9 - 1, dy = (lane / 3) % 3 - 1, dx = lane % 3 - 1;
+  for (int u = find_cell(C, cell_key(c[0] + dx, c[1] + dy, c[2] + dz)); u >= 0; u = C.next[u])
+    if (u != v && is_pair(C, v, u)) f(u);
+}
+__device__ __forceinline__ int warp_sum(int x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+__device__ __forceinline__ int warp_excl_scan(int x, int lane) {
+  int y = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, y, o);
+    if (lane >= o) y += t;
+  }
+  return y - x;
+}
+__device__ void c_count_warp(const ColView& C, int v, int lane) {
+  int all = 0, gt = 0;
+  if (is_surface(C, v)) warp_partners(C, v, lane, [&](int u) { all++; gt += u > v; });
+  all = warp_sum(all);
+  gt = warp_sum(gt);
+  if (lane == 0) {
+    C.cntAll[v] = all;
+    C.cntGt[v] = gt;
+  }
+}
+// v's partners, ascending, into the contact list and (for partners after v) the pair list.  The
+// lanes' partners are packed into the warp's shared buffer (exclusive scan of the lanes' counts),
+// then each element's place is its rank among them (the partners are distinct voxels).
+__device__ void c_fill_warp(const ColView& C, int v, int lane, int* sbuf /* kMaxPartners, this warp's */) {
+  if (!is_surface(C, v)) return;  // the same for the whole warp
+  int mine = 0;
+  warp_partners(C, v, lane, [&](int) { mine++; });
+  const int off = warp_excl_scan(mine, lane), n = warp_sum(mine);
   if (n > kMaxPartners) {
-    atomicOr(&C.cc->status, VXG_COL_ST_LOCAL_OVERFLOW);
+    if (lane == 0) atomicOr(&C.cc->status, VXG_COL_ST_LOCAL_OVERFLOW);
     return;
   }
-  for (int i = 1; i < n; ++i) {  // insertion sort, ascending
-    int x = buf[i], j = i - 1;
-    while (j >= 0 && buf[j] > x) { buf[j + 1] = buf[j]; --j; }
-    buf[j + 1] = x;
-  }
-  int wo = C.watchOff[v], po = C.pairOff[v], r = 0;
+  int k = off;
+  warp_partners(C, v, lane, [&](int u) { sbuf[k++] = u; });
+  __syncwarp();
+  int less = 0;  // partners before v in index order
+  for (int i = lane; i < n; i += 32) less += sbuf[i] < v;
+  const int nLess = warp_sum(less);
+  const int wo = C.watchOff[v], po = C.pairOff[v];
   const vxg_voxel_material& m1 = C.vm[C.vmat[v]];
-  for (int i = 0; i < n; ++i) {
-    int u = buf[i];
-    C.watchPartner[wo + i] = u;
+  for (int i = lane; i < n; i += 32) {
+    const int u = sbuf[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) r += sbuf[j] < u;
+    C.watchPartner[wo + r] = u;
     if (u > v) {
       const vxg_voxel_material& m2 = C.vm[C.vmat[u]];
-      int c = po + r++;
+      const int c = po + (r - nLess);
       C.pairI[c] = v;
       C.pairJ[c] = u;
       // CVX_Collision::CVX_Collision  VX_Collision.cpp:17-23
@@ -328,27 +364,23 @@ __device__ void c_fill_one(const ColView& C, int v) {
       C.pairDamp[c] = 0.5f * (m1.zetaCollision * m1.c2xSqMxExS + m2.zetaCollision * m2.c2xSqMxExS);
     }
   }
+  __syncwarp();  // the buffer is reused by this warp's next voxel
 }
-__global__ void c_fill(ColView C) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c_rebuilding(C) && !C.cc->status && i < C.cc->nsurf) c_fill_one(C, C.surf[i]);
-}
-
-__device__ void c_watch_one(const ColView& C, int v) {
-  if (v >= C.nv) return;
-  int wo = C.watchOff[v], n = C.cntAll[v];
-  int nLess = n - C.cntGt[v];
-  for (int k = 0; k < n; ++k) {
-    int u = C.watchPartner[wo + k];
+// each partner's pair index in v's contact list, the partners of one voxel side by side
+__device__ void c_watch_warp(const ColView& C, int v, int lane) {
+  const int wo = C.watchOff[v], n = C.cntAll[v];
+  const int nLess = n - C.cntGt[v];
+  for (int k = lane; k < n; k += 32) {
+    const int u = C.watchPartner[wo + k];
     int item;
     if (u > v) {
       item = (C.pairOff[v] + (k - nLess)) * 2;
     } else {
-      int uo = C.watchOff[u], ul = C.cntAll[u] - C.cntGt[u];
+      const int uo = C.watchOff[u], ul = C.cntAll[u] - C.cntGt[u];
       const int* seg = C.watchPartner + uo + ul;
       int lo = 0, hi = C.cntGt[u];
       while (lo < hi) {
-        int mid = (lo + hi) >> 1;
+        const int mid = (lo + hi) >> 1;
         if (seg[mid] < v) lo = mid + 1;
         else hi = mid;
       }
@@ -357,15 +389,39 @@ __device__ void c_watch_one(const ColView& C, int v) {
     C.watchItem[wo + k] = item;
   }
 }
+// the surface list's voxels, one per warp, warps striding over the list
+#define C_FOR_SURFACE_WARP(C, first_thread, threads, body)                                         \
+  do {                                                                                           \
+    const int lane_ = threadIdx.x & 31;                                                          \
+    const int ns_ = (C).cc->nsurf;                                                               \
+    for (int i_ = (first_thread) >> 5; i_ < ns_; i_ += (threads) >> 5) {                         \
+      const int v_ = (C).surf[i_];                                                               \
+      body(v_, lane_);                                                                           \
+    }                                                                                            \
+  } while (0)
+
+__global__ void c_count(ColView C) {
+  if (!c_rebuilding(C)) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  C_FOR_SURFACE_WARP(C, t, gridDim.x * blockDim.x, [&](int v, int lane) { c_count_warp(C, v, lane); });
+}
+__global__ void __launch_bounds__(256) c_fill(ColView C) {
+  __shared__ int sbuf[8][kMaxPartners];
+  if (!c_rebuilding(C) || C.cc->status) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  C_FOR_SURFACE_WARP(C, t, gridDim.x * blockDim.x, [&](int v, int lane) { c_fill_warp(C, v, lane, sbuf[threadIdx.x >> 5]); });
+}
 __global__ void c_watch(ColView C) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c_rebuilding(C) && !C.cc->status && i < C.cc->nsurf) c_watch_one(C, C.surf[i]);
+  if (!c_rebuilding(C) || C.cc->status) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  C_FOR_SURFACE_WARP(C, t, gridDim.x * blockDim.x, [&](int v, int lane) { c_watch_warp(C, v, lane); });
 }
 
 // The whole rebuild in one cooperative launch: the phases above, separated by grid-wide barriers
 // (a cooperative launch keeps every block resident, so the barriers end).  When the list is not
 // stale every block returns at once, so a step pays one launch instead of six.
 __global__ void __launch_bounds__(256) c_rebuild(ColView C) {
+  __shared__ int sbuf[8][kMaxPartners];  // c_fill_warp's buffer, one per warp
   if (!c_rebuilding(C)) return;  // uniform: no block reaches a barrier unless all do
   cooperative_groups::grid_group grid = cooperative_groups::this_grid();
   const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
@@ -374,15 +430,15 @@ __global__ void __launch_bounds__(256) c_rebuild(ColView C) {
   grid.sync();
   for (int i = first; i < ns; i += stride) c_insert_one(C, C.surf[i]);
   grid.sync();
-  for (int i = first; i < ns; i += stride) c_count_one(C, C.surf[i]);
+  C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_count_warp(C, v, lane); });
   grid.sync();
   if (blockIdx.x == 0) c_scan_block(C);
   grid.sync();
   if (C.cc->status) return;  // written before the last barrier: the same for every block
-  for (int i = first; i < ns; i += stride) c_fill_one(C, C.surf[i]);
+  C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_fill_warp(C, v, lane, sbuf[threadIdx.x >> 5]); });
   grid.sync();
   if (C.cc->status) return;
-  for (int i = first; i < ns; i += stride) c_watch_one(C, C.surf[i]);
+  C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_watch_warp(C, v, lane); });
 }
 
 // CVX_Voxel::baseSizeAverage for the envelope  VX_Voxel.h:90
@@ -443,10 +499,10 @@ __device__ void c_contact32(const ColView& C, int c, int a, int b) {
 __device__ __forceinline__ void c_contact64(const ColView& C, int c, int a, int b);
 // the contact forces of every listed pair, thread t of `threads`; thread 0 also closes the step's
 // bookkeeping (rebuild count, stale words, status to the control block)
-__device__ __forceinline__ void c_contact_all(const ColView& C, int t, int threads) {
+__device__ __forceinline__ void c_contact_all(const ColView& C, int t, int threads, bool rebuilt) {
   const int npairs = C.cc->npairs, status = C.cc->status;  // thread 0 clears neither
   if (t == 0) {
-    if (C.cc->stale) C.cc->rebuilds += 1;
+    if (rebuilt) C.cc->rebuilds += 1;
     C.cc->stale = 0;
     C.cc->force_stale = 0;
     if (status) atomicOr(&C.ctl->status, status << 8);
@@ -460,43 +516,54 @@ __device__ __forceinline__ void c_contact_all(const ColView& C, int t, int threa
 }
 __global__ void c_contact(ColView C) {
   if (C.ctl->halt || C.ctl->diverged) return;
-  c_contact_all(C, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+  c_contact_all(C, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, C.cc->stale != 0);
 }
 
 // The whole stage in one cooperative launch: the stale test, the rebuild phases when it found the
 // list stale, the contact forces, separated by grid-wide barriers (a cooperative launch keeps
 // every block resident, so the barriers end; every branch around a barrier reads words that
 // were written before the previous barrier, so all blocks take it alike).
-// full: the first step of a batch (the stale test over the surface list); otherwise the vote of
-// the previous step's voxel pass decides.
-__global__ void __launch_bounds__(256) c_stage(ColView C, int full) {
+// full: the first step of a batch (the stale test over the surface list, then a grid barrier);
+// otherwise the vote of the previous step's voxel pass decides, read by every block from words no
+// block of this launch writes before the decision is taken (force_stale is cleared only at the end,
+// after the rebuild's barriers when it was set; vote[parity ^ 1] not at all), so all blocks take
+// the same branch, and a step with nothing stale passes no barrier.
+__global__ void __launch_bounds__(256) c_stage(ColView C, int full, int parity) {
+  __shared__ int sbuf[8][kMaxPartners];  // c_fill_warp's buffer, one per warp
   if (C.ctl->halt || C.ctl->diverged) return;  // uniform: set before this launch
   cooperative_groups::grid_group grid = cooperative_groups::this_grid();
   const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   const int ns = C.cc->nsurf;
-  if (first == 0) {
-    if (C.cc->force_stale || (!full && C.cc->vote)) C.cc->stale = 1;
-    C.cc->vote = 0;
+  bool stale;
+  if (full) {
+    if (first == 0) {
+      if (C.cc->force_stale) C.cc->stale = 1;
+      C.cc->vote[parity] = 0;
+    }
+    if (__syncthreads_or(c_moved_listed(C, first, stride)) && threadIdx.x == 0) C.cc->stale = 1;
+    grid.sync();
+    stale = C.cc->stale != 0;
+  } else {
+    stale = C.cc->force_stale || C.cc->vote[parity ^ 1];
+    if (first == 0) C.cc->vote[parity] = 0;
   }
-  if (full && __syncthreads_or(c_moved_listed(C, first, stride)) && threadIdx.x == 0) C.cc->stale = 1;
-  grid.sync();
-  if (C.cc->stale) {
+  if (stale) {
     c_clear_range(C, first, stride);
     grid.sync();
     for (int i = first; i < ns; i += stride) c_insert_one(C, C.surf[i]);
     grid.sync();
-    for (int i = first; i < ns; i += stride) c_count_one(C, C.surf[i]);
+    C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_count_warp(C, v, lane); });
     grid.sync();
     if (blockIdx.x == 0) c_scan_block(C);
     grid.sync();
     if (!C.cc->status)
-      for (int i = first; i < ns; i += stride) c_fill_one(C, C.surf[i]);
+      C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_fill_warp(C, v, lane, sbuf[threadIdx.x >> 5]); });
     grid.sync();
     if (!C.cc->status)
-      for (int i = first; i < ns; i += stride) c_watch_one(C, C.surf[i]);
+      C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_watch_warp(C, v, lane); });
     grid.sync();
   }
-  c_contact_all(C, first, stride);
+  c_contact_all(C, first, stride, stale);
 }
 __device__ __forceinline__ void c_contact64(const ColView& C, int c, int a, int b) {
   const int nv = C.nv;
@@ -573,7 +640,7 @@ struct Collide {
     size_t o_last = take(sizeof(float) * 3 * (size_t)n);
     size_t o_hkey = take(8 * hcap), o_hhead = take(4 * hcap);
     size_t o_next = take(4 * (size_t)n), o_cg = take(4 * (size_t)n), o_ca = take(4 * (size_t)n);
-    size_t o_surf = take(4 * (size_t)n);
+    size_t o_surf = take(4 * (size_t)n), o_spos = take(24 * (size_t)n), o_scell = take(12 * (size_t)n);
     size_t o_po = take(4 * ((size_t)n + 1)), o_wo = take(4 * ((size_t)n + 1));
     size_t o_wp = take(4 * (size_t)wcap), o_wi = take(4 * (size_t)wcap);
     size_t o_pi = take(4 * (size_t)pcap), o_pj = take(4 * (size_t)pcap), o_ps = take(4 * (size_t)pcap),
@@ -591,6 +658,8 @@ struct Collide {
     C.cntGt = (int*)(buf + o_cg);
     C.cntAll = (int*)(buf + o_ca);
     C.surf = (int*)(buf + o_surf);
+    C.spos = (double*)(buf + o_spos);
+    C.scell = (int*)(buf + o_scell);
     C.pairOff = (int*)(buf + o_po);
     C.watchOff = (int*)(buf + o_wo);
     C.watchPartner = (int*)(buf + o_wp);
@@ -655,9 +724,9 @@ struct Collide {
   }
   // the View a voxel pass gets when collisions are on: it votes for the next step's stage
   bool ready() const { return buf && C.nbOff; }
-  void voted(View& S, const vxg_globals& g) {
+  void voted(View& S, const vxg_globals& g, int parity) {
     set_globals(g);
-    S.colVote = ready() ? &cc->vote : nullptr;
+    S.colVote = ready() ? &cc->vote[parity & 1] : nullptr;
     S.colLast = C.lastWatch;
     S.colRecalc2 = C.recalc2;
     S.colS = C.s64;
@@ -709,7 +778,7 @@ struct Collide {
     c_insert<<<gv, 256, 0, s>>>(C);
     c_count<<<gv, 256, 0, s>>>(C);
     c_scan<<<1, 1024, 0, s>>>(C);
-    c_fill<<<std::max(1, (nv + 127) / 128), 128, 0, s>>>(C);  // 128 threads: 512 B of partners each
+    c_fill<<<gv, 256, 0, s>>>(C);
     c_watch<<<gv, 256, 0, s>>>(C);
     return 6;
   }
@@ -734,19 +803,19 @@ struct Collide {
   }
   // full: the stale test itself (the first step of a batch or captured chunk); otherwise the vote
   // of the previous step's voxel pass
-  int enqueue(const vxg_globals& g, cudaStream_t s, bool full) {
+  int enqueue(const vxg_globals& g, cudaStream_t s, bool full, int parity) {
     if (!buf || !C.nbOff) return 0;
     set_globals(g);
-    int fl = full ? 1 : 0;
+    int fl = full ? 1 : 0, par = parity & 1;
     const int gs = stage_grid();
     if (gs > 0) {
-      void* args[] = {&C, &fl};
+      void* args[] = {&C, &fl, &par};
       if (cudaLaunchCooperativeKernel((const void*)c_stage, dim3(gs), dim3(256), args, 0, s) == cudaSuccess) return 1;
       cudaGetLastError();
       stage_blocks = 0;  // not available here: the separate kernels from now on
     }
     int gv = std::max(1, (nv + 255) / 256);
-    c_check<<<gv, 256, 0, s>>>(C, fl);
+    c_check<<<gv, 256, 0, s>>>(C, fl, par);
     int n = enqueue_rebuild(s);
     c_contact<<<grid_pairs, 256, 0, s>>>(C);
     return 2 + n;

@@ -1639,7 +1639,7 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   View Sv = S;
   vx32::View Vv = e->V;
   if (e->g.collisions && e->col.ready()) {
-    e->col.voted(Sv, e->g);
+    e->col.voted(Sv, e->g, parity);
     Vv.B = Sv;
   }
   bool rec = dt < 0;
@@ -1710,7 +1710,7 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
       }
     }
     if (ev) pass_event(ev[1], e->stream);
-    if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream, first);
+    if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream, first, parity);
     if (ev) pass_event(ev[2], e->stream);
     e->n_launch += nk;
     const bool voxel_pdl = pdl_base && e->nl && e->lp_bps == 0 && !e->g.collisions;
@@ -1729,7 +1729,7 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
     else k_link<false, true><<<gl, bl, 0, e->stream>>>(S, parity);
   }
   if (ev) pass_event(ev[1], e->stream);
-  if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream, first);
+  if (e->g.collisions) nk += e->col.enqueue(e->g, e->stream, first, parity);
   if (ev) pass_event(ev[2], e->stream);
   e->n_launch += nk;
   if (e->dec_mode) {  // one row of branch decisions per step (vxg_step checked the capacity)

@@ -75,8 +75,8 @@ def fp32c_bytes(n_voxels: int, n_links: int, poisson: bool, large_angle_links: i
 # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
 # 128x128x64 lattice, FP32C, warm step (profiles/fp32c_lattice128x128x64_dram.md), per unit
 MEASURED_TRAFFIC = {
-    "fp32c_link": {"per_voxel": 0.0, "per_link": 135.5},    # k_link32
-    "fp32c_voxel": {"per_voxel": 330.4, "per_link": 0.0},   # k_voxel32 with the Poisson fill
+    "fp32c_link": {"per_voxel": 0.0, "per_link": 134.5},    # k_link32
+    "fp32c_voxel": {"per_voxel": 332.3, "per_link": 0.0},   # k_voxel32 with the Poisson fill
 }
 
 
