@@ -96,3 +96,35 @@ def test_queued_temperatures_around_ambient_temperature(product_lib, cr_oracle):
         s.set_force(3, 0.0, 0.0, -0.001)
         assert s.do_time_steps(10, dt) == 10
     assert state_diff(g, o) == []
+
+
+@pytest.mark.parametrize("batch", [1, 7])
+def test_fp32c_temperatures_rest_lengths_in_the_link_pass(product_lib, batch):
+    """FP32C: the rest lengths of temperatures set with vx_set_temperatures are recomputed by the
+    next step's link pass when that step is launched on its own (batch 1), and by a rest-length pass
+    otherwise (a captured batch of 7), always as CVX_Voxel::setTemperature leaves them
+    (src/VX_Voxel.cpp:108-114, src/VX_Link.cpp:137-140).  Against a twin whose rest lengths are read
+    back (which brings them up to date) before every batch, the whole state is identical bit for
+    bit after every batch; a Poisson-ratio lattice covers the Poisson branch of the link pass."""
+    import ctypes as C
+
+    from conftest import state_diff
+
+    sc = S.lattice(14, 10, 8)
+    a = make_sim(product_lib, "vx", sc)
+    b = make_sim(product_lib, "vx", sc)
+    for s in (a, b):
+        F.Engine(s).set_precision(1)
+    dt = a.recommended_time_step()
+    b.recommended_time_step()
+    st = product_lib.vx_set_temperatures
+    st.argtypes = [C.c_void_p, C.c_void_p]
+    rng = np.random.default_rng(11)
+    nv = a.voxel_count()
+    for k in range(6):
+        temps = np.ascontiguousarray(rng.uniform(-0.5, 0.5, nv).astype(np.float32))
+        for s in (a, b):
+            assert st(C.c_void_p(s.h), temps.ctypes.data) == 0
+        b.link_state()  # reads the rest lengths: the separate rest-length pass runs first
+        assert a.do_time_steps(batch, dt) == b.do_time_steps(batch, dt) == batch
+        assert state_diff(a, b) == [], f"after batch {k}"

@@ -46,6 +46,7 @@ enum { VXG_COL_ST_PAIR_OVERFLOW = 1, VXG_COL_ST_WATCH_OVERFLOW = 2, VXG_COL_ST_L
        VXG_COL_ST_HASH_FULL = 8 };
 
 constexpr int kMaxPartners = 128;
+constexpr int kScanBlocks = 4096;  // most blocks a cooperative stage launch may have
 
 struct ColView {
   int nv;
@@ -74,6 +75,8 @@ struct ColView {
   int* cntAll;               // nv
   int* surf;                 // nv: the surface voxels (c_surface), nsurf of them
   double* spos;              // 3 nv: a surface voxel's position at the rebuild (cpos), set by c_insert
+  unsigned char* lcnt;       // 32 nv: partners lane k found in v's k-th neighbour cell (c_count)
+  int* part;                 // 2 kScanBlocks: per-block totals of the grid-wide scan
   int* scell;                // 3 nv: its hash-grid cell coordinates, set by c_insert
   int* pairOff;              // nv + 1
   int* watchOff;             // nv + 1
@@ -322,6 +325,9 @@ __device__ __forceinline__ int warp_excl_scan(int x, int lane) {
 __device__ void c_count_warp(const ColView& C, int v, int lane) {
   int all = 0, gt = 0;
   if (is_surface(C, v)) warp_partners(C, v, lane, [&](int u) { all++; gt += u > v; });
+  // each lane's own count, for the fill phase's offsets (a count over 255 means more partners than
+  // the fill phase accepts in total; it then reports the overflow)
+  C.lcnt[(size_t)v * 32 + lane] = (unsigned char)min(all, 255);
   all = warp_sum(all);
   gt = warp_sum(gt);
   if (lane == 0) {
@@ -330,12 +336,12 @@ __device__ void c_count_warp(const ColView& C, int v, int lane) {
   }
 }
 // v's partners, ascending, into the contact list and (for partners after v) the pair list.  The
-// lanes' partners are packed into the warp's shared buffer (exclusive scan of the lanes' counts),
-// then each element's place is its rank among them (the partners are distinct voxels).
+// lanes' partners are packed into the warp's shared buffer (exclusive scan of the lane counts the
+// count phase stored), then each element's place is its rank among them (the partners are
+// distinct voxels).
 __device__ void c_fill_warp(const ColView& C, int v, int lane, int* sbuf /* kMaxPartners, this warp's */) {
   if (!is_surface(C, v)) return;  // the same for the whole warp
-  int mine = 0;
-  warp_partners(C, v, lane, [&](int) { mine++; });
+  const int mine = C.lcnt[(size_t)v * 32 + lane];  // what this lane found in the count phase
   const int off = warp_excl_scan(mine, lane), n = warp_sum(mine);
   if (n > kMaxPartners) {
     if (lane == 0) atomicOr(&C.cc->status, VXG_COL_ST_LOCAL_OVERFLOW);
@@ -417,6 +423,84 @@ __global__ void c_watch(ColView C) {
   C_FOR_SURFACE_WARP(C, t, gridDim.x * blockDim.x, [&](int v, int lane) { c_watch_warp(C, v, lane); });
 }
 
+// Exclusive scans of cntGt -> pairOff and cntAll -> watchOff over all voxels by the whole grid of a
+// cooperative launch (256 threads per block): each block sums its contiguous share, a grid barrier,
+// then each block adds the totals of the blocks before it and scans its share in coalesced tiles.
+// Leaves the totals (pair and contact-list counts, overflow bits) in the control words; the caller
+// puts a grid barrier after it.
+__device__ __forceinline__ int block_sum256(int x, int* sh /* 8 */) {
+  x = warp_sum(x);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
+  __syncthreads();
+  int r = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) r += sh[k];
+  return r;
+}
+// exclusive scan across the block; *total = the block's sum
+__device__ __forceinline__ int block_excl_scan256(int x, int* sh /* 8 */, int* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int e = warp_excl_scan(x, lane);
+  __syncthreads();
+  if (lane == 31) sh[w] = e + x;
+  __syncthreads();
+  int before = 0, all = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    before += k < w ? sh[k] : 0;
+    all += sh[k];
+  }
+  *total = all;
+  return before + e;
+}
+__device__ void c_scan_grid(const ColView& C, cooperative_groups::grid_group& grid) {
+  __shared__ int sh[8];
+  const int nv = C.nv, G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
+  const int chunk = (nv + G - 1) / G;
+  const int lo = min(nv, b * chunk), hi = min(nv, lo + chunk);
+  int g = 0, a = 0;
+  for (int i = lo + t; i < hi; i += blockDim.x) {
+    g += C.cntGt[i];
+    a += C.cntAll[i];
+  }
+  g = block_sum256(g, sh);
+  a = block_sum256(a, sh);
+  if (t == 0) {
+    C.part[2 * b] = g;
+    C.part[2 * b + 1] = a;
+  }
+  grid.sync();
+  int og = 0, oa = 0;
+  for (int k = t; k < b; k += blockDim.x) {
+    og += C.part[2 * k];
+    oa += C.part[2 * k + 1];
+  }
+  og = block_sum256(og, sh);
+  oa = block_sum256(oa, sh);
+  for (int base = lo; base < hi; base += blockDim.x) {
+    const int i = base + t;
+    const int xg = i < hi ? C.cntGt[i] : 0, xa = i < hi ? C.cntAll[i] : 0;
+    int tg, ta;
+    const int eg = block_excl_scan256(xg, sh, &tg);
+    const int ea = block_excl_scan256(xa, sh, &ta);
+    if (i < hi) {
+      C.pairOff[i] = og + eg;
+      C.watchOff[i] = oa + ea;
+    }
+    og += tg;
+    oa += ta;
+  }
+  if (b == G - 1 && t == 0) {  // the last block's running offsets are the totals
+    C.pairOff[nv] = og;
+    C.watchOff[nv] = oa;
+    C.cc->npairs = og;
+    C.cc->nwatch = oa;
+    if (og > C.pcap) atomicOr(&C.cc->status, VXG_COL_ST_PAIR_OVERFLOW);
+    if (oa > C.wcap) atomicOr(&C.cc->status, VXG_COL_ST_WATCH_OVERFLOW);
+  }
+}
+
 // The whole rebuild in one cooperative launch: the phases above, separated by grid-wide barriers
 // (a cooperative launch keeps every block resident, so the barriers end).  When the list is not
 // stale every block returns at once, so a step pays one launch instead of six.
@@ -432,7 +516,7 @@ __global__ void __launch_bounds__(256) c_rebuild(ColView C) {
   grid.sync();
   C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_count_warp(C, v, lane); });
   grid.sync();
-  if (blockIdx.x == 0) c_scan_block(C);
+  c_scan_grid(C, grid);
   grid.sync();
   if (C.cc->status) return;  // written before the last barrier: the same for every block
   C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_fill_warp(C, v, lane, sbuf[threadIdx.x >> 5]); });
@@ -554,7 +638,7 @@ __global__ void __launch_bounds__(256) c_stage(ColView C, int full, int parity) 
     grid.sync();
     C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_count_warp(C, v, lane); });
     grid.sync();
-    if (blockIdx.x == 0) c_scan_block(C);
+    c_scan_grid(C, grid);
     grid.sync();
     if (!C.cc->status)
       C_FOR_SURFACE_WARP(C, first, stride, [&](int v, int lane) { c_fill_warp(C, v, lane, sbuf[threadIdx.x >> 5]); });
@@ -641,6 +725,7 @@ struct Collide {
     size_t o_hkey = take(8 * hcap), o_hhead = take(4 * hcap);
     size_t o_next = take(4 * (size_t)n), o_cg = take(4 * (size_t)n), o_ca = take(4 * (size_t)n);
     size_t o_surf = take(4 * (size_t)n), o_spos = take(24 * (size_t)n), o_scell = take(12 * (size_t)n);
+    size_t o_lcnt = take(32 * (size_t)n), o_part = take(8 * (size_t)kScanBlocks);
     size_t o_po = take(4 * ((size_t)n + 1)), o_wo = take(4 * ((size_t)n + 1));
     size_t o_wp = take(4 * (size_t)wcap), o_wi = take(4 * (size_t)wcap);
     size_t o_pi = take(4 * (size_t)pcap), o_pj = take(4 * (size_t)pcap), o_ps = take(4 * (size_t)pcap),
@@ -660,6 +745,8 @@ struct Collide {
     C.surf = (int*)(buf + o_surf);
     C.spos = (double*)(buf + o_spos);
     C.scell = (int*)(buf + o_scell);
+    C.lcnt = (unsigned char*)(buf + o_lcnt);
+    C.part = (int*)(buf + o_part);
     C.pairOff = (int*)(buf + o_po);
     C.watchOff = (int*)(buf + o_wo);
     C.watchPartner = (int*)(buf + o_wp);
@@ -757,7 +844,7 @@ struct Collide {
       cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
       if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c_rebuild, 256, 0) == cudaSuccess && per_sm > 0)
-        coop_blocks = std::min(n_sm * per_sm, std::max(1, (nv + 255) / 256));
+        coop_blocks = std::min(std::min(n_sm * per_sm, kScanBlocks), std::max(1, (nv + 255) / 256));
       else
         coop_blocks = 0;
       cudaGetLastError();
@@ -794,7 +881,7 @@ struct Collide {
       cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
       if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c_stage, 256, 0) == cudaSuccess && per_sm > 0)
-        stage_blocks = std::min(n_sm * per_sm, std::max(1, (nv + 255) / 256));
+        stage_blocks = std::min(std::min(n_sm * per_sm, kScanBlocks), std::max(1, (nv + 255) / 256));
       else
         stage_blocks = 0;
       cudaGetLastError();

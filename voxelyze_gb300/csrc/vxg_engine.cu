@@ -930,6 +930,9 @@ struct vxg_engine {
   // small-angle kernel needs as many registers as the general one, and the second launch made the
   // step slower, 0.150 against 0.144 ms on the 128x128x64 lattice)
   int link_split = 0;
+  // FP32C: temperatures the host set (vxg_set_temperatures, vxg_set_all_temperatures) whose links'
+  // rest lengths are not recomputed yet; the next step's link pass or a rest-length pass does it
+  bool rest_pending = false;
   int lL_grid = 0;  // grid of the general pass over deferred links (resident blocks on every SM)
   int n_sm = 0;
   bool tab_poisson = false;  // some voxel material has nu != 0
@@ -1071,10 +1074,17 @@ static void ensure32(vxg_engine* e) {
     if (e->dirty64 & (1u << f)) conv(e, f, 1);
   e->dirty64 = 0;
 }
+// FP32C: the rest lengths of temperatures the host set, before anything reads or copies them
+static void flush_rest(vxg_engine* e) {
+  if (!e->rest_pending) return;
+  if (e->nl) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
+  e->rest_pending = false;
+}
 // FP32C: refresh the FP64 copy of one field (or all with f < 0) before it is read
 static void ensure64(vxg_engine* e, int f = -1) {
   if (e->precision != VXG_FP32C) return;
   uint32_t want = f < 0 ? e->stale64 : (e->stale64 & (1u << f));
+  if (want & (1u << VXG_F_REST_LENGTH)) flush_rest(e);
   for (int k = 0; k < VXG_F_COUNT; ++k)
     if (want & (1u << k)) conv(e, k, 0);
   e->stale64 &= ~want;
@@ -1266,6 +1276,7 @@ int vxg_resize(vxg_engine* e, int nv, int nl) {
   VXG_CK(cudaSetDevice(e->device));
   VXG_CK(cudaStreamSynchronize(e->stream));
   release_arena(e);
+  e->rest_pending = false;
   // decision rows are sized by the voxel count: a new scene starts without them
   if (e->d_dec) cudaFree(e->d_dec);
   e->d_dec = nullptr;
@@ -1323,6 +1334,8 @@ int vxg_set_field(vxg_engine* e, int f, const void* host, long long count) {
   long long n = (long long)d.comps * (d.per_link ? e->nl : e->nv);
   if (count != n) return fail(e, VXG_E_SIZE, "vxg_set_field: element count mismatch");
   if (n == 0) return VXG_OK;
+  if (f == VXG_F_REST_LENGTH) e->rest_pending = false;  // the host's rest lengths win
+  else flush_rest(e);  // from the temperatures as they were set, before any field changes
   e->poisson_redo = true;
   if (f == VXG_F_VOXEL_MATERIAL || f == VXG_F_VOXEL_LINKS || f == VXG_F_VOXEL_EXTERNAL ||
       f == VXG_F_LINK_VOXELS || f == VXG_F_LINK_MATERIAL)
@@ -1411,6 +1424,7 @@ int vxg_set_temperatures_sparse(vxg_engine* e, int n, const int* voxels, const f
   for (int i = 0; i < n; ++i)
     if (voxels[i] < 0 || voxels[i] >= e->nv) return fail(e, VXG_E_ARG, "vxg_set_temperatures_sparse: voxel index out of range");
   VXG_CK(cudaSetDevice(e->device));
+  flush_rest(e);  // the sparse update recomputes only the edited voxels' links
   if (n > e->n_sp_cap) {
     if (e->d_sp_idx) cudaFree(e->d_sp_idx);
     if (e->d_sp_t) cudaFree(e->d_sp_t);
@@ -1475,6 +1489,7 @@ int vxg_mesh_update(vxg_engine* e, float* vertices, float* normals) {
   NvtxScope nvtx("vxg_mesh_update");
   if (!e) return VXG_E_ARG;
   VXG_CK(cudaSetDevice(e->device));
+  flush_rest(e);
   if (int rc = check_topology(e)) return rc;
   ensure32(e);  // FP32C: host-written state first
   const int nvt = e->n_mesh_vert, nq = e->n_mesh_quad;
@@ -1581,6 +1596,12 @@ static void pass_event(cudaEvent_t ev, cudaStream_t s) {
 static bool fused_poisson(const vxg_engine* e) {
   return e->precision == VXG_FP32C && e->tab_poisson && e->poisson_fuse;
 }
+// FP32C at a fixed dt with the default one-kernel link pass and no Poisson pre-pass: the link pass
+// can recompute the rest lengths from the temperatures itself (k_link32<..., ACT = true>)
+static bool link_recomputes_rest(const vxg_engine* e, bool rec) {
+  return e->precision == VXG_FP32C && e->nl && !rec && e->lp_bps == 0 && !e->link_split &&
+         !(e->g.any_poisson && !fused_poisson(e));
+}
 // before a batch: the Poisson caches the FP32C voxel pass filled ahead, after a host edit
 static void poisson_refill(vxg_engine* e) {
   if (fused_poisson(e) && e->poisson_redo && e->g.any_poisson && e->nv) {
@@ -1633,7 +1654,10 @@ inline void launch_pdl(bool pdl, void (*kernel)(KArgs...), int grid, int block, 
 }
 }
 
-static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEvent_t* ev = nullptr) {
+// rest_first: host-set temperatures not yet in the rest lengths; the step's link pass recomputes them
+// (the caller only passes it where link_recomputes_rest holds)
+static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEvent_t* ev = nullptr,
+                         bool rest_first = false) {
   const View& S = e->S;
   // the voxel pass's View: with collisions on it votes on the next step's stale test
   View Sv = S;
@@ -1656,8 +1680,8 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   const bool pdl_base = e->pdl && !ev && e->precision == VXG_FP32C;
   // FP32C at a fixed dt with the default link pass: the actuation's rest-length update happens in
   // the link pass itself (k_link32<..., ACT>), which directly follows the actuation kernel
-  const bool act_fused = e->act_mode && e->nv && e->nl && e->precision == VXG_FP32C && !rec && e->lp_bps == 0 &&
-                         !e->link_split && !(e->g.any_poisson && !fused_poisson(e));
+  const bool act_fused = e->act_mode && e->nv && link_recomputes_rest(e, rec);
+  const bool link_act = act_fused || (rest_first && link_recomputes_rest(e, rec));
   bool link_pdl = pdl_base && !first && (!e->act_mode || act_fused);
   long long nk = 1 + (e->nl ? 1 : 0) + (e->act_mode && e->nv ? 1 + (e->nl && !act_fused ? 1 : 0) : 0) +
                  (e->g.any_poisson && e->nv && !fused_poisson(e) ? 1 : 0);
@@ -1701,7 +1725,7 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
           launch_pdl(pdl_base, k_link32L<false>, gL, 256, e->stream, e->V);
         }
         nk += 1;
-      } else if (act_fused) {
+      } else if (link_act) {
         if (pois) launch_pdl(link_pdl, k_link32<false, true, true, true>, gl, bl, e->stream, e->V, parity);
         else launch_pdl(link_pdl, k_link32<false, true, false, true>, gl, bl, e->stream, e->V, parity);
       } else {
@@ -1795,6 +1819,10 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
     return fail(e, VXG_E_SIZE, "vxg_step: more steps than the branch-decision rows set aside");
   // branch decisions take a row pointer per step: launched step by step, never captured
   bool use_graph = e->timing != 1 && nsteps > 1 && !e->dec_mode;
+  // temperatures the host set since the last step: the first step's link pass recomputes the rest
+  // lengths where it is launched on its own with the default link pass, else a pass does it now
+  const bool rest_first = e->rest_pending && !use_graph && e->timing != 1 && link_recomputes_rest(e, dt < 0);
+  if (!rest_first) flush_rest(e);
   const int chunk = e->graph_chunk;
   // capture and instantiate the batch's graph before the batch timer starts (timing mode 2 times
   // the replay, not the capture)
@@ -1857,7 +1885,8 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
     if (c != cudaSuccess) return fail(e, VXG_E_CUDA, "timed batch", c);
     e->tev_used = nsteps;
   } else {
-    for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == 0);
+    for (int s = 0; s < nsteps; ++s) enqueue_step(e, dt, s & 1, s == 0, nullptr, rest_first && s == 0);
+    e->rest_pending = false;
   }
   if (e->timing == 2) VXG_CK(cudaEventRecord(e->bev[1], e->stream));
   if (!e->h_ctl) VXG_CK(cudaMallocHost(&e->h_ctl, 4 * sizeof(int)));
@@ -2015,6 +2044,7 @@ int vxg_recommended_dt(vxg_engine* e, float* dt) {
   if (!e || !dt) return VXG_E_ARG;
   if (!e->have_globals) return fail(e, VXG_E_STATE, "vxg_set_globals was not called");
   VXG_CK(cudaSetDevice(e->device));
+  flush_rest(e);
   if (int rc = check_topology(e)) return rc;
   int zeros[4] = {0, 0, 0, 0};
   VXG_CK(cudaMemcpyAsync(e->ctl, zeros, sizeof(zeros), cudaMemcpyHostToDevice, e->stream));
@@ -2046,7 +2076,7 @@ int vxg_set_all_temperatures(vxg_engine* e, float t) {
   ensure32(e);
   if (e->nv) k_set_temp<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->S, t);
   if (e->precision == VXG_FP32C) {
-    if (e->nl) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
+    e->rest_pending = true;  // the next step's link pass (or a rest-length pass) recomputes them
     e->stale64 |= 1u << VXG_F_REST_LENGTH;
   } else if (e->nl) {
     k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
@@ -2061,7 +2091,7 @@ int vxg_set_temperatures(vxg_engine* e, const float* t) {
   ensure32(e);
   if (e->nv) VXG_CK(cudaMemcpyAsync(e->S.temp, t, sizeof(float) * (size_t)e->nv, cudaMemcpyHostToDevice, e->stream));
   if (e->precision == VXG_FP32C) {
-    if (e->nl) k_rest32<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->V);
+    e->rest_pending = true;  // the next step's link pass (or a rest-length pass) recomputes them
     e->stale64 |= 1u << VXG_F_REST_LENGTH;
   } else if (e->nl) {
     k_rest_length<<<grid_for(e->nl), kBlock, 0, e->stream>>>(e->S);
@@ -2234,6 +2264,7 @@ int vxg_snapshot(vxg_engine* e, int slot) {
   if (!e || slot < 0 || slot > 1023) return VXG_E_ARG;
   VXG_CK(cudaSetDevice(e->device));
   ensure32(e);
+  flush_rest(e);
   if ((int)e->snaps.size() <= slot) e->snaps.resize(slot + 1);
   vxg_engine::Snap& sl = e->snaps[slot];
   const size_t sizes[4] = {e->arena_bytes, e->arena32_bytes, sizeof(Ctl), e->col.buf_bytes};
@@ -2270,6 +2301,7 @@ int vxg_restore(vxg_engine* e, int slot) {
     e->dirty64 = 0;
     e->stale64 = all_state_bits();
   }
+  e->rest_pending = false;  // snapshots are taken with the rest lengths up to date
   e->poisson_redo = true;
   return VXG_OK;
 }
