@@ -328,7 +328,7 @@ def run_ours(args, world, rank, local):
         blk = E.launch()
         launch[name] = {"block_link": blk[0], "block_voxel": blk[1], "graph_chunk": blk[2],
                         "link_pipeline": E.link_pipeline(), "link_split": E.link_split(),
-                        "autotuned": not args.no_autotune}
+                        "body_batch_voxels": E.body_batches()[0], "autotuned": not args.no_autotune}
     for sim in (sim64, sim32):
         if sim.do_time_steps(args.warmup, dt) != args.warmup:
             raise RuntimeError("warm-up diverged")

@@ -123,6 +123,8 @@ int vx_set_link_pipeline(void* s, int blocks_per_sm);                      /* vx
 int vx_get_link_pipeline(void* s, int* blocks_per_sm);                     /* vxg_get_link_pipeline */
 int vx_set_link_split(void* s, int on);                                    /* vxg_set_link_split */
 int vx_get_link_split(void* s, int* on);                                   /* vxg_get_link_split */
+int vx_set_body_batches(void* s, int voxels_per_group);                    /* vxg_set_body_batches */
+int vx_get_body_batches(void* s, int* voxels_per_group, int* groups);      /* vxg_get_body_batches */
 int vx_set_poisson_fusion(void* s, int on);                                /* vxg_set_poisson_fusion */
 /* the engine behind a handle (include/vxg.h), pending host edits uploaded first; NULL on failure.
  * No counterpart in the reference: for callers that mix the engine ABI with this facade. */

@@ -223,6 +223,20 @@ int vxg_get_link_pipeline(vxg_engine* e, int* blocks_per_sm);
  * both. */
 int vxg_set_link_split(vxg_engine* e, int on);
 int vxg_get_link_split(vxg_engine* e, int* on);
+/* Body batches (no counterpart in the reference, which steps one scene per CVoxelyze): for a scene
+ * of many bodies that no link joins, FP32C at a fixed dt without collisions.  The voxel order is cut
+ * wherever no link spans the cut; consecutive pieces are packed into groups of up to
+ * voxels_per_group voxels (1: every piece its own group; 0, the default: off), and each vxg_step
+ * batch runs in one persistent launch whose CTAs take the groups largest first and run each
+ * through every step of the batch (in-step actuation, links, voxels, with block barriers), so a
+ * group's state stays in L2 across the steps.  Needs the links in the order of their pieces (a scene
+ * built body after body) and at least one group per SM; otherwise batches run as passes.  Results
+ * are bit-identical either way: each CTA first copies its group's slice of every array a step
+ * writes, and a batch in which a group diverges is put back and run again as passes.
+ * vxg_autotune compares group sizes with the passes.  `groups` (optional): the groups of the
+ * current scene. */
+int vxg_set_body_batches(vxg_engine* e, int voxels_per_group);
+int vxg_get_body_batches(vxg_engine* e, int* voxels_per_group, int* groups);
 /* Branch decisions of the FP64 voxel pass (no counterpart in the reference), for finite differences
  * that follow one run's branches: mode 1 records, for each of the next `steps` steps, every voxel's
  * floor-contact and static-friction decisions (CVX_Voxel::floorForce and the static-friction latch

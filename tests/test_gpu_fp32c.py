@@ -282,3 +282,107 @@ def test_positions_into_pinned_memory(product_lib):
         assert read(s.h, staged.ctypes.data) == 0
         assert np.array_equal(pinned.numpy(), staged)
         assert np.array_equal(staged.reshape(3, -1).T, s.voxel_state()["pos"])
+
+
+def _launches(lib, sim):
+    import ctypes as C
+
+    cnt = (C.c_longlong * 8)()
+    assert lib.vx_counters(C.c_void_p(sim.h), cnt, 8) == 0
+    return int(cnt[6])
+
+
+def _bodies_scene(kind):
+    """300 small bodies (3 to 6 cells a side) on the floor with friction, two materials (one with
+    CTE); 'poisson': both materials with nu = 0.3 (the Poisson cache filled by the voxel phase)."""
+    sc = S.population(300, 3, 6, seed=11)
+    if kind == "poisson":
+        for m in sc.materials:
+            m.nu = 0.3
+    return sc
+
+
+def _packed_groups(sizes, target):
+    """Groups of consecutive bodies of these voxel counts, each up to `target` voxels (a larger
+    body alone): the packing vxg_set_body_batches describes."""
+    groups, cur = 0, 0
+    for n in sizes:
+        if cur and cur + n > target:
+            groups, cur = groups + 1, 0
+        cur += n
+    return groups + 1
+
+
+@pytest.mark.parametrize("kind", ["plain", "uniform_actuation", "phase_actuation", "poisson"])
+def test_body_batches_are_bit_identical(product_lib, kind):
+    """vxg_set_body_batches: each batch in one persistent launch whose CTAs take groups of bodies
+    through every step (actuation, links, voxels, block barriers), against the default two passes
+    per step replayed from CUDA graphs; every state array identical bit for bit after batches of
+    1, 50 and 130 steps, and the time.  The body batch is checked to have run (two launches per
+    batch) with one group per body (voxels per group 1: 300 groups) and with consecutive bodies
+    packed up to 100 voxels to a group (196 groups, more than the SMs)."""
+    from conftest import state_diff
+
+    sc = _bodies_scene(kind)
+    for target in (1, 100):
+        a, b = (make_sim(product_lib, "vx", sc) for _ in range(2))
+        for s in (a, b):
+            E = F.Engine(s)
+            E.set_precision(1)
+            if kind == "uniform_actuation":
+                E.set_actuation(F.ACT_UNIFORM, 0.2, 3.0)
+            elif kind == "phase_actuation":
+                ph = np.random.default_rng(3).uniform(0, 2 * np.pi, sc.n_voxels).astype(np.float32)
+                E.set_actuation(F.ACT_PER_VOXEL, 0.2, 3.0, ph)
+        Eb = F.Engine(b)
+        Eb.set_body_batches(target)
+        per_group, groups = Eb.body_batches()
+        assert per_group == target
+        assert groups == _packed_groups(np.bincount(sc.body), target)
+        dt = a.recommended_time_step()
+        assert b.recommended_time_step() == dt
+        for n in (1, 50, 130):
+            l0 = _launches(product_lib, b)
+            assert a.do_time_steps(n, dt) == b.do_time_steps(n, dt) == n
+            assert _launches(product_lib, b) - l0 == 2, "the body batch did not run"
+            assert state_diff(a, b) == [], f"after a batch of {n} (voxels per group {target})"
+        assert a.current_time() == b.current_time()
+
+
+def test_body_batch_divergence_is_rolled_back(product_lib):
+    """One body pulled by a force far too large for it (src/Voxelyze.cpp:263-269): the body batch
+    in which its links diverge is put back and run again as passes, which stop at the same step as
+    the passes of a second simulator, with every other body at that step too (links advanced,
+    voxels not); one more batch after it matches as well."""
+    from conftest import state_diff
+
+    sc = _bodies_scene("plain")
+    sc.force_idx = np.array([int(np.flatnonzero(sc.body == 7)[0])])
+    sc.force_val = np.array([[3e4, 0.0, 1e4]], np.float32)
+    a, b = (make_sim(product_lib, "vx", sc) for _ in range(2))
+    for s in (a, b):
+        F.Engine(s).set_precision(1)
+    F.Engine(b).set_body_batches(1)
+    dt = a.recommended_time_step()
+    b.recommended_time_step()
+    assert a.do_time_steps(1, dt) == b.do_time_steps(1, dt) == 1
+    na, nb = a.do_time_steps(200, dt), b.do_time_steps(200, dt)
+    assert 1 <= na == nb < 200
+    assert state_diff(a, b) == []
+    assert a.current_time() == b.current_time()
+    assert a.do_time_steps(3, dt) == b.do_time_steps(3, dt)
+    assert state_diff(a, b) == []
+
+
+def test_body_batches_need_separate_bodies(product_lib):
+    """A single connected lattice is one piece: no group per SM, so batches run as passes."""
+    sc = S.lattice(20, 16, 10)
+    b = make_sim(product_lib, "vx", sc)
+    E = F.Engine(b)
+    E.set_precision(1)
+    E.set_body_batches(1)
+    assert E.body_batches() == (1, 1)
+    dt = b.recommended_time_step()
+    l0 = _launches(product_lib, b)
+    assert b.do_time_steps(10, dt) == 10
+    assert _launches(product_lib, b) - l0 > 2

@@ -1603,6 +1603,16 @@ int vx_get_link_split(void* s, int* on) {
   if (!vx.upload()) return -1;
   return vxg_get_link_split(vx.impl()->eng, on) ? -1 : 0;
 }
+int vx_set_body_batches(void* s, int voxels_per_group) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_set_body_batches(vx.impl()->eng, voxels_per_group) ? -1 : 0;
+}
+int vx_get_body_batches(void* s, int* voxels_per_group, int* groups) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_get_body_batches(vx.impl()->eng, voxels_per_group, groups) ? -1 : 0;
+}
 int vx_set_poisson_fusion(void* s, int on) {
   CVoxelyze& vx = H(s)->vx;
   if (!vx.upload()) return -1;

@@ -451,11 +451,16 @@ VX_HDN float link_compute(const View& S, int l, const LinkIn& in, float ipdt) {
   return link_compute_t<false>(S, l, in, ipdt, nullptr);
 }
 
+// ipdt: 1 / the dt every voxel stepped with last
 template <bool POIS, bool ACT = false>
-VX_HDN float link_update(const View& S, int l) {
+VX_HDN float link_update_ip(const View& S, int l, float ipdt) {
   const LinkIn in = link_gather<POIS, ACT>(S, l);
   if (ACT) S.restDelta[l] = in.rd;
-  return link_compute(S, l, in, S.B.ctl->inv_last_dt);  // every voxel stepped with last_dt
+  return link_compute(S, l, in, ipdt);
+}
+template <bool POIS, bool ACT = false>
+VX_HDN float link_update(const View& S, int l) {
+  return link_update_ip<POIS, ACT>(S, l, S.B.ctl->inv_last_dt);
 }
 
 // The small-angle form for link l whose flags lf the caller has read and found small-angle:

@@ -410,6 +410,8 @@ _EXT_SIGS = {
     "set_link_pipeline": (_i, [_p, _i]),
     "get_link_pipeline": (_i, [_p, _ip]),
     "set_link_split": (_i, [_p, _i]),
+    "set_body_batches": (_i, [_p, _i]),
+    "get_body_batches": (_i, [_p, _ip, _ip]),
     "get_link_split": (_i, [_p, _ip]),
     "set_decisions": (_i, [_p, _i, C.c_longlong]),
     "get_decisions": (_i, [_p, C.POINTER(C.c_ubyte), C.c_longlong]),
@@ -471,6 +473,18 @@ class Engine:
         """FP32C link pass at a fixed dt: the small-angle kernel plus the general kernel over the
         links it defers, or the general kernel over every link (default); identical results."""
         self._ck(self.f["set_link_split"](self.sim.h, 1 if on else 0))
+
+    def set_body_batches(self, voxels_per_group: int):
+        """FP32C, fixed dt, no collisions, bodies no link joins: each batch in one persistent launch
+        whose CTAs run groups of bodies (up to voxels_per_group voxels; 1: one body per group;
+        0: off) through every step; identical results."""
+        self._ck(self.f["set_body_batches"](self.sim.h, int(voxels_per_group)))
+
+    def body_batches(self) -> tuple[int, int]:
+        """(voxels per group, groups of the current scene)."""
+        out = np.zeros(2, np.int32)
+        self._ck(self.f["get_body_batches"](self.sim.h, _ptr(out[:1], C.c_int), _ptr(out[1:], C.c_int)))
+        return int(out[0]), int(out[1])
 
     def link_split(self) -> bool:
         out = np.zeros(1, np.int32)
