@@ -81,6 +81,8 @@ int vx_link_is_failed(void* s, int l);                      /* CVX_Link::isFaile
 /* extensions for throughput users */
 int vx_set_precision(void* s, int mode);                    /* 0 = FP64 (default), 1 = FP32C */
 int vx_read_positions(void* s, double* xyz);                /* 3 n_voxels doubles, component-major, straight from the GPU */
+int vx_read_positions_async(void* s, double* xyz);          /* the same, copied while later steps run: vxg_read_positions_async */
+int vx_read_wait(void* s);                                  /* every vx_read_positions_async has landed: vxg_read_wait */
 int vx_set_temperatures(void* s, const float* t);           /* n_voxels floats: every voxel's setTemperature */
 float vx_state_info_device(void* s, int info, int type);    /* GPU reduction, see vxg_reduce */
 /* stateInfo (info, type as vx_state_info; not PRESSURE) reduced on the GPU and written as one float

@@ -155,6 +155,15 @@ int vxg_resize(vxg_engine* e, int n_voxels, int n_links);
  * naming the field and element, and nothing runs. */
 int vxg_set_field(vxg_engine* e, int field, const void* host, long long count);
 int vxg_get_field(vxg_engine* e, int field, void* host, long long count);
+/* Every voxel's position (VXG_F_POS: 3 n_voxels doubles, component-major) read without waiting:
+ * the positions as of this call are converted into one of two device staging buffers on the
+ * engine's stream and copied to `host` on a second stream, so the copy runs while later steps
+ * compute.  `host` is written once vxg_read_wait returns (pinned host memory for the copy to
+ * overlap; pageable memory makes the call wait for it).  A third read reuses the first staging
+ * buffer once its copy has left.  No counterpart in the reference, whose positions are host
+ * memory (CVX_Voxel::position, include/VX_Voxel.h:131). */
+int vxg_read_positions_async(vxg_engine* e, double* host);
+int vxg_read_wait(vxg_engine* e);
 int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const vxg_link_material* lm,
                    int n_lm, const vxg_external* ext, int n_ext);
 /* Uploads only the externals table (the layout and slot numbering of vxg_set_tables), after

@@ -284,6 +284,78 @@ def test_positions_into_pinned_memory(product_lib):
         assert np.array_equal(staged.reshape(3, -1).T, s.voxel_state()["pos"])
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_async_position_reads(product_lib, precision):
+    """vx_read_positions_async: each step's positions are staged on the device and copied while the
+    next steps run; after vx_read_wait every buffer holds exactly what a synchronous read after
+    that step returned (a second simulator stepping alongside), for pinned and pageable buffers,
+    for more reads in flight than staging buffers, and across a change of the scene's size."""
+    import torch
+
+    sc = S.lattice(24, 20, 10)
+    a, b = (make_sim(product_lib, "vx", sc) for _ in range(2))
+    for s in (a, b):
+        F.Engine(s).set_precision(precision)
+    Eb = F.Engine(b)
+    dt = a.recommended_time_step()
+    b.recommended_time_step()
+    n = 3 * a.voxel_count()
+    bufs = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() if k % 3 else np.zeros(n)
+            for k in range(7)]
+    want = []
+    for k in range(7):
+        assert a.do_time_steps(3, dt) == b.do_time_steps(3, dt) == 3
+        want.append(F.Engine(a).read_positions().T.reshape(-1).copy())
+        Eb.read_positions_async(bufs[k])
+    Eb.read_wait()
+    for k in range(7):
+        assert np.array_equal(bufs[k], want[k]), f"read {k}"
+    nv = b.voxel_count()
+    b.set_voxel(0, 40, 40, 0)
+    assert b.voxel_count() == nv + 1
+    out = np.zeros(3 * b.voxel_count())
+    assert b.do_time_steps(2, dt) == 2
+    Eb.read_positions_async(out)
+    Eb.read_wait()
+    assert np.array_equal(out, Eb.read_positions().T.reshape(-1))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_temperatures_from_pinned_memory(product_lib, precision):
+    """vx_set_temperatures from pinned host memory is read by a kernel (16-byte loads where the
+    buffer is aligned, single floats where not) instead of a copy: the same state bit for bit as
+    temperatures from pageable memory, on a voxel count that is not a multiple of four."""
+    import ctypes as C
+
+    import torch
+
+    from conftest import state_diff
+
+    sc = S.lattice(13, 11, 7)
+    sims = [make_sim(product_lib, "vx", sc) for _ in range(3)]
+    for s in sims:
+        F.Engine(s).set_precision(precision)
+    nv = sims[0].voxel_count()
+    assert nv % 4 != 0
+    set_t = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)(("vx_set_temperatures", product_lib))
+    rng = np.random.default_rng(5)
+    dt = sims[0].recommended_time_step()
+    for s in sims[1:]:
+        s.recommended_time_step()
+    pinned = torch.empty(nv + 1, dtype=torch.float32, pin_memory=True)
+    for _ in range(4):
+        t = rng.uniform(-20, 20, nv).astype(np.float32)
+        pinned[:nv] = torch.from_numpy(t)
+        assert set_t(sims[0].h, t.ctypes.data) == 0
+        assert set_t(sims[1].h, pinned.data_ptr()) == 0
+        pinned[1:] = torch.from_numpy(t)
+        assert set_t(sims[2].h, pinned.data_ptr() + 4) == 0  # 4 bytes past a 16-byte boundary
+        for s in sims:
+            assert s.do_time_steps(3, dt) == 3
+    assert state_diff(sims[0], sims[1]) == []
+    assert state_diff(sims[0], sims[2]) == []
+
+
 def _launches(lib, sim):
     import ctypes as C
 

@@ -1449,6 +1449,16 @@ int vx_read_positions(void* s, double* xyz) {
   CVoxelyze& vx = H(s)->vx;
   return vx.readField(VXG_F_POS, xyz, 3ll * vx.voxelCount()) ? 0 : -1;
 }
+int vx_read_positions_async(void* s, double* xyz) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.upload()) return -1;
+  return vxg_read_positions_async(vx.impl()->eng, xyz) ? -1 : 0;
+}
+int vx_read_wait(void* s) {
+  CVoxelyze& vx = H(s)->vx;
+  if (!vx.impl()->eng) return 0;
+  return vxg_read_wait(vx.impl()->eng) ? -1 : 0;
+}
 int vx_set_temperatures(void* s, const float* t) { return H(s)->vx.setTemperatures(t) ? 0 : -1; }
 float vx_state_info_device(void* s, int info, int type) {
   return H(s)->vx.stateInfoDevice((CVoxelyze::stateInfoType)info, (CVoxelyze::valueType)type);

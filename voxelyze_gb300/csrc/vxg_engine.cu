@@ -142,6 +142,22 @@ __global__ void k_set_temp(View S, float t) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v < S.nv) S.temp[v] = t;
 }
+// every voxel's temperature read straight from host memory the device can address (pinned),
+// 16 bytes a thread where both ends allow it
+__global__ void k_temp_in(View S, const float* src) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = S.nv;
+  const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(S.temp)) & 15) == 0;
+  if (vec) {
+    if (4 * i + 3 < nv) {
+      reinterpret_cast<float4*>(S.temp)[i] = reinterpret_cast<const float4*>(src)[i];
+    } else {
+      for (int v = 4 * i; v < nv; ++v) S.temp[v] = src[v];
+    }
+  } else if (i < nv) {
+    S.temp[i] = src[i];
+  }
+}
 __global__ void k_rest_length(View S) {
   int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= S.nl) return;
@@ -966,6 +982,14 @@ struct vxg_engine {
   int precision = VXG_FP64;
   int nv = 0, nl = 0;
   cudaStream_t stream = nullptr;
+  // vxg_read_positions_async: two device staging buffers (3 nv doubles each), copied to the host on
+  // their own stream while later steps run; a buffer is reused only after its last copy has left
+  cudaStream_t cstream = nullptr;
+  double* d_stage[2] = {nullptr, nullptr};
+  size_t stage_bytes = 0;
+  cudaEvent_t ev_staged[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+  bool stage_used[2] = {false, false};
+  int stage_next = 0;
   char* arena = nullptr;
   size_t arena_bytes = 0;
   void* field_ptr[VXG_F_COUNT] = {};
@@ -1371,6 +1395,15 @@ int vxg_destroy(vxg_engine* e) {
   for (cudaEvent_t x : e->tev) cudaEventDestroy(x);
   for (cudaEvent_t x : e->bev) if (x) cudaEventDestroy(x);
   if (e->h_ctl) cudaFreeHost(e->h_ctl);
+  if (e->cstream) {
+    cudaStreamSynchronize(e->cstream);
+    cudaStreamDestroy(e->cstream);
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (e->d_stage[k]) cudaFree(e->d_stage[k]);
+    if (e->ev_staged[k]) cudaEventDestroy(e->ev_staged[k]);
+    if (e->ev_copied[k]) cudaEventDestroy(e->ev_copied[k]);
+  }
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return VXG_OK;
@@ -1484,6 +1517,55 @@ int vxg_get_field(vxg_engine* e, int f, void* host, long long count) {
   if (is_state_field(f)) ensure64(e, f);
   VXG_CK(cudaMemcpyAsync(host, e->field_ptr[f], (size_t)n * d.elem, cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
+  return VXG_OK;
+}
+
+int vxg_read_positions_async(vxg_engine* e, double* host) {
+  if (!e || (!host && e->nv)) return VXG_E_ARG;
+  if (!e->nv) return VXG_OK;
+  VXG_CK(cudaSetDevice(e->device));
+  const size_t bytes = sizeof(double) * 3 * (size_t)e->nv;
+  if (!e->cstream) {
+    VXG_CK(cudaStreamCreateWithFlags(&e->cstream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      VXG_CK(cudaEventCreateWithFlags(&e->ev_staged[k], cudaEventDisableTiming));
+      VXG_CK(cudaEventCreateWithFlags(&e->ev_copied[k], cudaEventDisableTiming));
+    }
+  }
+  if (e->stage_bytes != bytes) {  // first use, or the scene changed size: copies in flight end first
+    VXG_CK(cudaStreamSynchronize(e->cstream));
+    for (int k = 0; k < 2; ++k) {
+      if (e->d_stage[k]) cudaFree(e->d_stage[k]);
+      e->d_stage[k] = nullptr;
+      e->stage_used[k] = false;
+    }
+    e->stage_bytes = 0;
+    for (int k = 0; k < 2; ++k) VXG_CK(cudaMalloc(&e->d_stage[k], bytes));
+    e->stage_bytes = bytes;
+  }
+  const int k = e->stage_next;
+  e->stage_next ^= 1;
+  if (e->stage_used[k]) VXG_CK(cudaStreamWaitEvent(e->stream, e->ev_copied[k], 0));
+  if (e->precision == VXG_FP32C && (e->stale64 & (1u << VXG_F_POS))) {
+    ensure32(e);
+    k_pos_out<<<grid_for(e->nv), kBlock, 0, e->stream>>>(e->V, e->g.voxSize, e->d_stage[k]);
+    VXG_CK(cudaGetLastError());
+  } else {
+    VXG_CK(cudaMemcpyAsync(e->d_stage[k], e->field_ptr[VXG_F_POS], bytes, cudaMemcpyDeviceToDevice, e->stream));
+  }
+  VXG_CK(cudaEventRecord(e->ev_staged[k], e->stream));
+  VXG_CK(cudaStreamWaitEvent(e->cstream, e->ev_staged[k], 0));
+  VXG_CK(cudaMemcpyAsync(host, e->d_stage[k], bytes, cudaMemcpyDeviceToHost, e->cstream));
+  VXG_CK(cudaEventRecord(e->ev_copied[k], e->cstream));
+  e->stage_used[k] = true;
+  return VXG_OK;
+}
+
+int vxg_read_wait(vxg_engine* e) {
+  if (!e) return VXG_E_ARG;
+  if (!e->cstream) return VXG_OK;
+  VXG_CK(cudaSetDevice(e->device));
+  VXG_CK(cudaStreamSynchronize(e->cstream));
   return VXG_OK;
 }
 
@@ -2360,7 +2442,18 @@ int vxg_set_temperatures(vxg_engine* e, const float* t) {
   if (!e || (!t && e->nv)) return VXG_E_ARG;
   VXG_CK(cudaSetDevice(e->device));
   ensure32(e);
-  if (e->nv) VXG_CK(cudaMemcpyAsync(e->S.temp, t, sizeof(float) * (size_t)e->nv, cudaMemcpyHostToDevice, e->stream));
+  if (e->nv) {
+    // pinned host memory: read by a kernel (no copy engine, which the overlapped position reads
+    // use); anything else: a copy
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, t) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+      const bool vec = ((reinterpret_cast<uintptr_t>(pa.devicePointer) | reinterpret_cast<uintptr_t>(e->S.temp)) & 15) == 0;
+      k_temp_in<<<grid_for(vec ? (e->nv + 3) / 4 : e->nv), kBlock, 0, e->stream>>>(e->S, (const float*)pa.devicePointer);
+    } else {
+      cudaGetLastError();
+      VXG_CK(cudaMemcpyAsync(e->S.temp, t, sizeof(float) * (size_t)e->nv, cudaMemcpyHostToDevice, e->stream));
+    }
+  }
   if (e->precision == VXG_FP32C) {
     e->rest_pending = true;  // the next step's link pass (or a rest-length pass) recomputes them
     e->stale64 |= 1u << VXG_F_REST_LENGTH;

@@ -394,6 +394,8 @@ class Sim:
 _EXT_SIGS = {
     "set_precision": (_i, [_p, _i]),
     "read_positions": (_i, [_p, _dp]),
+    "read_positions_async": (_i, [_p, _dp]),
+    "read_wait": (_i, [_p]),
     "set_temperatures": (_i, [_p, _fp]),
     "state_info_device": (_f, [_p, _i, _i]),
     "counters": (_i, [_p, C.POINTER(C.c_longlong), _i]),
@@ -544,3 +546,14 @@ class Engine:
         out = np.zeros(3 * n, np.float64)
         self._ck(self.f["read_positions"](self.sim.h, _ptr(out, C.c_double)))
         return out.reshape(3, n).T
+
+    def read_positions_async(self, out: np.ndarray):
+        """Start copying every voxel's position into ``out`` (3 n float64, component-major) while
+        later steps run; ``out`` holds them once read_wait() returns.  The copy overlaps only for
+        pinned memory (a numpy array waits for it)."""
+        if out.dtype != np.float64 or out.size != 3 * self.sim.voxel_count() or not out.flags.c_contiguous:
+            raise ValueError("needs a contiguous float64 array of 3 * voxel_count() elements")
+        self._ck(self.f["read_positions_async"](self.sim.h, _ptr(out, C.c_double)))
+
+    def read_wait(self):
+        self._ck(self.f["read_wait"](self.sim.h))
