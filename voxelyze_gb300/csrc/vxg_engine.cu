@@ -2773,6 +2773,42 @@ int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* 
   }
   e->graph_chunk = bc;
   e->graph_valid = false;
+  // The per-pass events above include each pass's launch gap and keep the passes from overlapping,
+  // which on small scenes is most of a pass: the shapes they picked, the plain link kernel at the
+  // same shapes, and the engine's defaults are compared once more as replayed batches
+  if (!rc && e->nl) {
+    struct Shape { int bl, bv, split, bps; };
+    const Shape picked = {e->blk_link, e->blk_voxel, e->link_split, e->lp_bps};
+    const Shape cands[3] = {picked, {picked.bl, picked.bv, 0, 0}, {e->precision == VXG_FP32C ? 128 : 256, 256, 0, 0}};
+    const int timing0 = e->timing;
+    float best_t = 1e30f;
+    Shape best_s = picked;
+    e->timing = 2;
+    for (int k = 0; k < 3 && !rc; ++k) {
+      const Shape& c = cands[k];
+      if (k && c.bl == picked.bl && c.bv == picked.bv && c.split == picked.split && c.bps == picked.bps) continue;
+      e->blk_link = c.bl;
+      e->blk_voxel = c.bv;
+      e->link_split = c.split;
+      e->lp_bps = c.bps;
+      e->graph_valid = false;
+      int done = 0, div = 0;
+      const int n = std::max(2 * bc, trial_steps);
+      if ((rc = vxg_step(e, n, dt, &done, &div))) break;  // captures or warms up
+      if ((rc = vxg_restore(e, slot))) break;
+      if ((rc = vxg_step(e, n, dt, &done, &div))) break;
+      if (e->t_batch < best_t) { best_t = e->t_batch; best_s = c; }
+      if ((rc = vxg_restore(e, slot))) break;
+    }
+    e->timing = timing0;
+    e->blk_link = best_s.bl;
+    e->blk_voxel = best_s.bv;
+    e->link_split = best_s.split;
+    e->lp_bps = best_s.bps;
+    e->graph_valid = false;
+    bl = best_s.bl;
+    bv = best_s.bv;
+  }
   // FP32C at a fixed dt: body batches of several group sizes (1: every segment a group of its own)
   // against the replayed graphs, on batches of the trial length
   if (!rc && e->precision == VXG_FP32C && dt > 0) {
