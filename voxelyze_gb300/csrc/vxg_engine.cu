@@ -1028,6 +1028,11 @@ struct vxg_engine {
   cudaGraphExec_t cgraph = nullptr;
   float cgraph_dt = 0;
   int cgraph_n = -1;
+  // single steps (a control loop calling one step at a time): the step captured as well, with and
+  // without the rest-length update of host-set temperatures in its link pass
+  cudaGraphExec_t g1[2] = {nullptr, nullptr};
+  float g1_dt[2] = {0, 0};
+  long long g1_kernels[2] = {0, 0};
   int graph_chunk = 64;
   // launch shapes (vxg_set_launch / vxg_autotune)
   int blk_link = 256, blk_voxel = 256;
@@ -1369,6 +1374,8 @@ int vxg_destroy(vxg_engine* e) {
   if (e->stream) cudaStreamSynchronize(e->stream);
   if (e->graph) cudaGraphExecDestroy(e->graph);
   if (e->cgraph) cudaGraphExecDestroy(e->cgraph);
+  for (cudaGraphExec_t g : e->g1)
+    if (g) cudaGraphExecDestroy(g);
   if (e->d_phase) cudaFree(e->d_phase);
   if (e->d_body_off) cudaFree(e->d_body_off);
   if (e->d_body_out) cudaFree(e->d_body_out);
@@ -2107,16 +2114,24 @@ static void enqueue_step(vxg_engine* e, float dt, int parity, bool first, cudaEv
   if (ev) pass_event(ev[3], e->stream);
 }
 
-static int capture(vxg_engine* e, int n, float dt, cudaGraphExec_t* out) {
+// every cached graph, after a change that any of them may have baked in
+static void drop_graphs(vxg_engine* e) {
+  for (cudaGraphExec_t* g : {&e->graph, &e->cgraph, &e->g1[0], &e->g1[1]})
+    if (*g) {
+      cudaGraphExecDestroy(*g);
+      *g = nullptr;
+    }
+  e->graph_n = e->cgraph_n = -1;
+}
+// rest_first: the first step's link pass recomputes the rest lengths (enqueue_step)
+static int capture(vxg_engine* e, int n, float dt, cudaGraphExec_t* out, long long* kernels, bool rest_first = false) {
   if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
   cudaGraph_t g;
   VXG_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
   const long long before = e->n_launch;
-  for (int s = 0; s < n; ++s) enqueue_step(e, dt, s & 1, s == 0);
-  const long long in_graph = e->n_launch - before;
+  for (int s = 0; s < n; ++s) enqueue_step(e, dt, s & 1, s == 0, nullptr, rest_first && s == 0);
+  *kernels = e->n_launch - before;
   e->n_launch = before;  // counted per replay
-  if (out == &e->cgraph) e->cgraph_kernels = in_graph;
-  else e->graph_kernels = in_graph;
   VXG_CK(cudaStreamEndCapture(e->stream, &g));
   cudaError_t c = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
@@ -2159,28 +2174,37 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
   if (bodies) use_graph = false;
   const bool rest_first = e->rest_pending && !bodies && !use_graph && e->timing != 1 && link_recomputes_rest(e, dt < 0);
   if (!rest_first) flush_rest(e);
+  // a single step is replayed from a captured step as well (one launch instead of the step's
+  // kernels), with the rest-length update in its link pass or without
+  const bool use_g1 = nsteps == 1 && e->timing != 1 && !e->dec_mode && !bodies;
+  const int g1k = rest_first ? 1 : 0;
   const int chunk = e->graph_chunk;
+  if ((use_graph || use_g1) && !e->graph_valid) {
+    drop_graphs(e);
+    e->graph_valid = true;
+  }
   // capture and instantiate the batch's graph before the batch timer starts (timing mode 2 times
   // the replay, not the capture)
   if (use_graph && nsteps >= chunk) {
     // long runs: one captured chunk (even length keeps the step parities aligned) replayed
-    if (!e->graph_valid || !e->cgraph || e->cgraph_dt != dt || e->cgraph_n != chunk) {
-      int rc = capture(e, chunk, dt, &e->cgraph);
+    if (!e->cgraph || e->cgraph_dt != dt || e->cgraph_n != chunk) {
+      int rc = capture(e, chunk, dt, &e->cgraph, &e->cgraph_kernels);
       if (rc) return rc;
       e->cgraph_dt = dt;
       e->cgraph_n = chunk;
-      if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
-      e->graph_n = -1;
-      e->graph_valid = true;
     }
   } else if (use_graph) {
-    if (!e->graph_valid || !e->graph || e->graph_n != nsteps || e->graph_dt != dt) {
-      int rc = capture(e, nsteps, dt, &e->graph);
+    if (!e->graph || e->graph_n != nsteps || e->graph_dt != dt) {
+      int rc = capture(e, nsteps, dt, &e->graph, &e->graph_kernels);
       if (rc) return rc;
       e->graph_n = nsteps;
       e->graph_dt = dt;
-      if (!e->graph_valid && e->cgraph) { cudaGraphExecDestroy(e->cgraph); e->cgraph = nullptr; }
-      e->graph_valid = true;
+    }
+  } else if (use_g1) {
+    if (!e->g1[g1k] || e->g1_dt[g1k] != dt) {
+      int rc = capture(e, 1, dt, &e->g1[g1k], &e->g1_kernels[g1k], rest_first);
+      if (rc) return rc;
+      e->g1_dt[g1k] = dt;
     }
   }
   if (e->timing == 2) {
@@ -2198,6 +2222,10 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
                                                           (int)e->body_cols.size());
     k_bodies_done<<<1, 32, 0, e->stream>>>(e->ctl, dt, nsteps, e->d_bctl);
     e->n_launch += 2;
+  } else if (use_g1) {
+    VXG_CK(cudaGraphLaunch(e->g1[g1k], e->stream));
+    e->n_launch += e->g1_kernels[g1k];
+    e->rest_pending = false;
   } else if (use_graph) {
     if (nsteps >= chunk) {
       int full = nsteps / chunk;
