@@ -243,6 +243,22 @@ int main() {
     in.Ml = D3(U(-1e-4, 1e-4), U(-1e-4, 1e-4), U(-1e-4, 1e-4));
     in.extF = D3(0, 0, 0);
     in.extM = D3(0, 0, 0);
+    // every third case an external that fixes some degrees of freedom (all but all six)
+    vxg_external ext;
+    std::memset(&ext, 0, sizeof(ext));
+    in.dof = 0;
+    in.fixPos = D3(0, 0, 0);
+    in.fixOrient = Q4(1, 0, 0, 0);
+    if (c % 3 == 1) {
+      static const int dofs[16] = {1, 2, 4, 3, 5, 6, 8, 16, 32, 24, 40, 48, 56, 7 | 8, 4 | 56, 1 | 32};
+      in.dof = dofs[rng() % 16];
+      ext.dof = in.dof;
+      for (int k = 0; k < 3; ++k) ext.translation[k] = U(-1e-4, 1e-4);
+      q4 r = small_rotation(0.3);
+      ext.rotq[0] = r.w; ext.rotq[1] = r.x; ext.rotq[2] = r.y; ext.rotq[3] = r.z;
+      in.fixPos = D3(ext.translation[0], ext.translation[1], ext.translation[2]);  // at lattice index 0
+      in.fixOrient = r;
+    }
     {  // the engine forward on a one-voxel View whose single link slot carries Fl, Ml
       vxg_voxel_material vm;
       std::memset(&vm, 0, sizeof(vm));
@@ -252,14 +268,14 @@ int main() {
       vm.muKinetic = in.muKinetic;
       vm.nomSize = L0;
       vm.size[0] = vm.size[1] = vm.size[2] = L0 + 2 * off;
-      int vlinks[6] = {0, -1, -1, -1, -1, -1}, vmat[1] = {0}, vidx[3] = {0, 0, 0}, vext[1] = {-1};
+      int vlinks[6] = {0, -1, -1, -1, -1, -1}, vmat[1] = {0}, vidx[3] = {0, 0, 0}, vext[1] = {in.dof ? 0 : -1};
       float temp[1] = {0}, prevDt[1] = {0};
       vx64::Ctl ctl;
       std::memset(&ctl, 0, sizeof(ctl));
       vx64::View S;
       std::memset(&S, 0, sizeof(S));
       S.nv = 1; S.nl = 1; S.vmat = vmat; S.vidx = vidx; S.vlinks = vlinks; S.vext = vext; S.temp = temp;
-      S.prevDt = prevDt; S.vm = &vm; S.ctl = &ctl;
+      S.prevDt = prevDt; S.vm = &vm; S.ctl = &ctl; S.ext = &ext;
       in.halfPenOffset = vx64::base_size_avg(S, 0) / 2 - vm.nomSize / 2;
       in.pos = D3(U(-0.1, 0.1), U(-0.1, 0.1), in.halfPenOffset + U(-3e-5, 3e-5));
       double pos[3] = {in.pos.x, in.pos.y, in.pos.z}, lin[3] = {in.lin.x, in.lin.y, in.lin.z},

@@ -1,8 +1,8 @@
 // Reverse-mode derivatives of one FP64 time step (link pass + voxel pass), hand-written.
 //
 // Scope of the differentiated step: linear link materials with Poisson's ratio 0 and no failure
-// strain, links in the small-angle branch (VX_Link.cpp:96-103), no voxel-voxel collisions,
-// externals that fix all six degrees of freedom or only add forces/moments; floor contact and
+// strain, links in the small-angle branch (VX_Link.cpp:96-103), no voxel-voxel collisions; externals
+// add forces and moments and fix any of the six degrees of freedom; floor contact and
 // static/kinetic friction are differentiated along the branch the forward pass took
 // (VX_Voxel.cpp:274-298 and the latch at :194-205).  Every forward quantity is recomputed here with
 // the arithmetic of vx_phys64.cuh from the state recorded at the start of the step; the derivative
@@ -417,6 +417,9 @@ struct VoxelIn {
       penetrationStiffness, muStatic, muKinetic;
   double halfPenOffset;  // base size average / 2 - nominal size / 2 (temperature dependent)
   d3 extF, extM;
+  int dof;               // the external's fixed degrees of freedom (bits 0-2 translation, 3-5 rotation)
+  d3 fixPos;             // the prescribed position and orientation of those degrees of freedom
+  q4 fixOrient;
 };
 struct VoxelOut {
   d3 pos, lin, ang;
@@ -424,7 +427,51 @@ struct VoxelOut {
   bool staticF;
 };
 
-// CVX_Voxel::timeStep without collisions and partial fixes (vx64::voxel_update's arithmetic)
+// the external's fixes at the end of CVX_Voxel::timeStep (VX_Voxel.cpp:215-229, vx64::voxel_update)
+VX_HD void apply_fixes(const VoxelIn& in, d3& pos, d3& lin, q4& orient, d3& ang) {
+  if (in.dof & 1) { pos.x = in.fixPos.x; lin.x = 0; }
+  if (in.dof & 2) { pos.y = in.fixPos.y; lin.y = 0; }
+  if (in.dof & 4) { pos.z = in.fixPos.z; lin.z = 0; }
+  if (in.dof & 56) {
+    if ((in.dof & 56) == 56) {
+      orient = in.fixOrient;
+      ang = D3(0, 0, 0);
+    } else {
+      d3 r = rotation_vector(orient);
+      if (in.dof & 8) { r.x = 0; ang.x = 0; }
+      if (in.dof & 16) { r.y = 0; ang.y = 0; }
+      if (in.dof & 32) { r.z = 0; ang.z = 0; }
+      orient = from_rotation_vector(r);
+    }
+  }
+}
+// Its adjoint: the adjoints of the state before the fixes from those after (q: the orientation
+// before them).  A fixed component's value does not depend on anything.
+VX_HD void apply_fixes_adj(const VoxelIn& in, const q4& q, d3& gpos, d3& glin, q4& gq, d3& gang) {
+  if (in.dof & 1) { gpos.x = 0; glin.x = 0; }
+  if (in.dof & 2) { gpos.y = 0; glin.y = 0; }
+  if (in.dof & 4) { gpos.z = 0; glin.z = 0; }
+  if (in.dof & 56) {
+    if ((in.dof & 56) == 56) {
+      gq = Q4(0, 0, 0, 0);
+      gang = D3(0, 0, 0);
+    } else {
+      d3 r = rotation_vector(q);
+      if (in.dof & 8) { r.x = 0; gang.x = 0; }
+      if (in.dof & 16) { r.y = 0; gang.y = 0; }
+      if (in.dof & 32) { r.z = 0; gang.z = 0; }
+      d3 gr = D3(0, 0, 0);
+      from_rotation_vector_adj(r, gq, gr);
+      if (in.dof & 8) gr.x = 0;
+      if (in.dof & 16) gr.y = 0;
+      if (in.dof & 32) gr.z = 0;
+      gq = Q4(0, 0, 0, 0);
+      rotation_vector_adj(q, gr, gq);
+    }
+  }
+}
+
+// CVX_Voxel::timeStep without collisions (vx64::voxel_update's arithmetic)
 VX_HD VoxelOut voxel_forward(const VoxelIn& in) {
   VoxelOut o;
   d3 lin = in.lin, ang = in.ang, pos = in.pos;
@@ -491,7 +538,9 @@ VX_HD VoxelOut voxel_forward(const VoxelIn& in) {
   ang.x += dt * M.x; ang.y += dt * M.y; ang.z += dt * M.z;
   float dti = dt * in.inertiaInv;
   q4 dq = from_rotation_vector(D3(dti * ang.x, dti * ang.y, dti * ang.z));
-  o.orient = vx64::qmul(dq, in.orient);
+  q4 orient = vx64::qmul(dq, in.orient);
+  apply_fixes(in, pos, lin, orient, ang);
+  o.orient = orient;
   o.pos = pos;
   o.lin = lin;
   o.ang = ang;
@@ -507,7 +556,7 @@ struct VoxelGrad {
 };
 
 // Adjoint of voxel_forward given the adjoints of the new state.
-VX_HD void voxel_adjoint(const VoxelIn& in, const d3& gpos_n, const d3& glin_n, const q4& gq_n, const d3& gang_n,
+VX_HD void voxel_adjoint(const VoxelIn& in, const d3& gpos_f, const d3& glin_f, const q4& gq_f, const d3& gang_f,
                          VoxelGrad& g) {
   // ---- forward recomputation ----
   const d3 lin0 = in.lin;
@@ -574,6 +623,10 @@ VX_HD void voxel_adjoint(const VoxelIn& in, const d3& gpos_n, const d3& glin_n, 
   q4 dq = from_rotation_vector(rv);
 
   // ---- reverse ----
+  // the external's fixes, last in the forward step, first here
+  d3 gpos_n = gpos_f, glin_n = glin_f, gang_n = gang_f;
+  q4 gq_n = gq_f;
+  if (in.dof) apply_fixes_adj(in, vx64::qmul(dq, in.orient), gpos_n, glin_n, gq_n, gang_n);
   g.gMass = g.gMassInv = g.gInertiaInv = g.gC2x = g.gC2xI = g.gPenStiff = g.gHalfPenOffset = 0;
   // orient' = dq * orient
   q4 gdq = Q4(0, 0, 0, 0);

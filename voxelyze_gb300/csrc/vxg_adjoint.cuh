@@ -192,10 +192,18 @@ __global__ void k_adj_voxel(View S, AdjBuf T, ActParams A, int slot, float dt) {
     in.halfPenOffset = bsa / 2 - m.nomSize / 2;
   }
   int ei = S.vext[v];
+  in.dof = 0;
+  in.fixPos = vx64::D3(0, 0, 0);
+  in.fixOrient = vx64::Q4(1, 0, 0, 0);
   if (ei >= 0) {
     const vxg_external& e = S.ext[ei];
     in.extF = vx64::D3(e.force[0], e.force[1], e.force[2]);
     in.extM = vx64::D3(e.moment[0], e.moment[1], e.moment[2]);
+    in.dof = e.dof & 0x3F;
+    const double s = m.nomSize;
+    in.fixPos = vx64::D3(S.vidx[v] * s + e.translation[0], S.vidx[nv + v] * s + e.translation[1],
+                         S.vidx[2 * nv + v] * s + e.translation[2]);
+    in.fixOrient = vx64::Q4(e.rotq[0], e.rotq[1], e.rotq[2], e.rotq[3]);
   } else {
     in.extF = in.extM = vx64::D3(0, 0, 0);
   }

@@ -1594,9 +1594,6 @@ int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const 
       e->adj_scope = "a link material is not linear, has Poisson's ratio != 0 or a failure strain";
   for (int k = 0; k < n_vm && !e->adj_scope; ++k)
     if (vm[k].nu != 0.0f) e->adj_scope = "a voxel material has Poisson's ratio != 0";
-  for (int k = 0; k < n_ext && !e->adj_scope; ++k)
-    if ((ext[k].dof & 0x3F) != 0 && (ext[k].dof & 0x3F) != 0x3F)
-      e->adj_scope = "an external fixes some but not all degrees of freedom";
   VXG_CK(cudaStreamSynchronize(e->stream));
   rebuild_view(e);
   return VXG_OK;

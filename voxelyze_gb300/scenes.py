@@ -44,6 +44,8 @@ class Scene:
     mats: np.ndarray          # (N,) material index per voxel, insertion order
     xyz: np.ndarray           # (N,3) lattice index per voxel
     fixed_all: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))   # voxel indices
+    fixed_idx: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))   # partial fixes:
+    fixed_mask: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))  # dofComponent bits
     force_idx: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     force_val: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.float32))
     gravity: float = 0.0
@@ -92,6 +94,8 @@ def apply(scene: Scene, sim: "F.Sim") -> None:
     sim.set_voxels(scene.mats, scene.xyz)
     for v in scene.fixed_all:
         sim.set_fixed_all(int(v), True)
+    for v, mask in zip(scene.fixed_idx, scene.fixed_mask):
+        sim.set_fixed(int(v), int(mask))
     for v, f in zip(scene.force_idx, scene.force_val):
         sim.set_force(int(v), float(f[0]), float(f[1]), float(f[2]))
 
