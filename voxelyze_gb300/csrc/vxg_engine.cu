@@ -756,6 +756,11 @@ __global__ void __launch_bounds__(kBodyCta, 1)
     }
   }
 }
+// the batch's first four control words (diverged, halt, steps, status) into mapped host memory
+__global__ void k_ctl_out(const vx64::Ctl* ctl, int* out) {
+  const int* w = reinterpret_cast<const int*>(ctl);
+  if (threadIdx.x < 4) out[threadIdx.x] = w[threadIdx.x];
+}
 // after k_bodies32: the control words of a batch that ran to its end (the voxel pass's updates,
 // step by step); a batch some group diverged in is flagged (diverged without halt) for the host,
 // which runs it again as passes.  Leaves the counter and the first diverged step for the next batch.
@@ -1071,7 +1076,10 @@ struct vxg_engine {
   bool pdl = true;           // FP32C passes launched to overlap the previous kernel's tail
   bool topo_ok = false;      // k_validate passed for the current index fields and tables
   unsigned long long* d_bad = nullptr;
-  int* h_ctl = nullptr;      // pinned copy of the batch's control words
+  // the batch's control words in mapped pinned memory, written there by a kernel (k_ctl_out) so that
+  // reading them never queues behind a large copy on a copy engine (vxg_read_positions_async)
+  int* h_ctl = nullptr;
+  int* h_ctl_dev = nullptr;
   // kernels launched by the time step (a graph replay counts the kernels it holds)
   long long n_launch = 0, graph_kernels = 0, cgraph_kernels = 0;
   // FP64 branch decisions (vxg_set_decisions): 0 off, 1 record, 2 replay; one byte per voxel per
@@ -2258,8 +2266,12 @@ int vxg_step(vxg_engine* e, int nsteps, float dt, int* steps_done, int* diverged
     e->rest_pending = false;
   }
   if (e->timing == 2) VXG_CK(cudaEventRecord(e->bev[1], e->stream));
-  if (!e->h_ctl) VXG_CK(cudaMallocHost(&e->h_ctl, 4 * sizeof(int)));
-  VXG_CK(cudaMemcpyAsync(e->h_ctl, e->ctl, 4 * sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  if (!e->h_ctl) {
+    VXG_CK(cudaHostAlloc(&e->h_ctl, 4 * sizeof(int), cudaHostAllocMapped));
+    VXG_CK(cudaHostGetDevicePointer(&e->h_ctl_dev, e->h_ctl, 0));
+  }
+  k_ctl_out<<<1, 32, 0, e->stream>>>(e->ctl, e->h_ctl_dev);
+  e->n_launch += 1;
   VXG_CK(cudaStreamSynchronize(e->stream));
   const int* h = e->h_ctl;
   VXG_CK(cudaGetLastError());
