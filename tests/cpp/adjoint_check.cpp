@@ -48,7 +48,9 @@ static void set_consts(LinkIn& in, const LinkConsts& c) {
 
 static const double L0 = 0.01;
 
-static LinkIn random_link() {
+// kind 0: small-angle; 1: large-angle, bent so that orientLink's frame comes from its near-x
+// formula; 2: large-angle, bent further (its general formula)
+static LinkIn random_link(int kind = 0) {
   LinkIn in;
   in.axis = (int)(rng() % 3);
   d3 e = D3(in.axis == 0, in.axis == 1, in.axis == 2);
@@ -66,6 +68,28 @@ static LinkIn random_link() {
   in.oldA2 = D3(U(-1e-2, 1e-2), U(-1e-2, 1e-2), U(-1e-2, 1e-2));
   in.rest = L0 * (1 + U(-1e-3, 1e-3));
   in.smallAngle = true;
+  if (kind) {
+    // kind 2: bent, the positive end displaced sideways by 0.2-0.5 of the length (the bend far past
+    // the hysteresis bound 1.2 x 0.05); kind 1: stretched by 60 % (past the extension bound 0.5)
+    // and barely bent, |y| and |z| below 1.732e-2 of x in the link frame (the near-x frame formula)
+    const double side = U(0.2, 0.5);
+    d3 off = D3(U(-1, 1), U(-1, 1), U(-1, 1));
+    d3 loc = D3(ext, side * ext * (off.y > 0 ? 1 : -1), side * ext * off.z);
+    if (kind == 1) {
+      const double x = 1.6 * ext;
+      loc = D3(x, 5e-3 * x * (off.y > 0 ? 1 : -1), 4e-3 * x * (off.z > 0 ? 1 : -1));
+      in.qn = base;
+    }
+    // loc in the link frame (x along the axis) to world axes
+    d3 w = in.axis == 0 ? loc : in.axis == 1 ? D3(loc.z, loc.x, loc.y) : D3(loc.y, loc.z, loc.x);
+    d3 dw = vx64::rotate(base, w);
+    in.pp = D3(in.pn.x + dw.x, in.pn.y + dw.y, in.pn.z + dw.z);
+    in.qp = vx64::qmul(small_rotation(0.3), base);
+    in.smallAngle = false;
+    in.oldA1 = D3(U(-0.2, 0.2), U(-0.2, 0.2), U(-0.2, 0.2));
+    in.oldA2 = D3(U(-0.2, 0.2), U(-0.2, 0.2), U(-0.2, 0.2));
+    in.oldPos2 = D3(U(-1e-4, 1e-4), 0, 0);
+  }
   in.lvv = rng() % 4 != 0;
   set_consts(in, link_consts((float)std::exp(U(std::log(3e5), std::log(3e6))), (float)L0));
   in.tArea = (float)(L0 * L0);
@@ -129,13 +153,14 @@ struct Check {
   double err = 0;
   int n = 0;
   int tag = 0;
+  double floor_frac = 1e-4;
   void row(const std::vector<double>& fd, const std::vector<double>& ad) {
     double big = 0;
     for (double x : ad) big = std::max(big, std::fabs(x));
     for (double x : fd) big = std::max(big, std::fabs(x));
     if (big == 0) return;
     for (size_t i = 0; i < fd.size(); ++i) {
-      double e = std::fabs(fd[i] - ad[i]) / std::max(std::max(std::fabs(fd[i]), std::fabs(ad[i])), 1e-4 * big);
+      double e = std::fabs(fd[i] - ad[i]) / std::max(std::max(std::fabs(fd[i]), std::fabs(ad[i])), floor_frac * big);
       if (e > err) {
         err = e;
         if (std::getenv("ADJ_VERBOSE")) printf("  %s worst so far: output %d input %zu fd %.9e ad %.9e\n", name, tag, i, fd[i], ad[i]);
@@ -146,7 +171,7 @@ struct Check {
 };
 
 static double link_out(const LinkOut& o, int k) {
-  const d3 O[6] = {o.fN, o.fP, o.mN, o.mP, o.pos2, o.a2v};
+  const d3 O[7] = {o.fN, o.fP, o.mN, o.mP, o.pos2, o.a1v, o.a2v};
   const double v[3] = {O[k / 3].x, O[k / 3].y, O[k / 3].z};
   return v[k % 3];
 }
@@ -159,38 +184,61 @@ static double voxel_out(const VoxelOut& o, int k) {
 int main() {
   int bad_forward = 0, link_cases = 0;
   Check cl{"link"};
-  for (int c = 0; c < 200; ++c) {
-    LinkIn in = random_link();
+  // large-angle links: strains of 0.1-0.6 and damping forces ~1e3 N make the differences of the
+  // smallest gradient components noisy, so their floor is 1e-3 of each output's largest component
+  Check cll{"link_large"};
+  cll.floor_frac = 1e-3;
+  int large_cases = 0;
+  for (int c = 0; c < 300; ++c) {
+    const int kind = c % 3;  // small-angle, large-angle near-x frame, large-angle general frame
+    LinkIn in = random_link(kind);
     LinkOut a = link_forward(in), b = engine_link(in);
-    if (b.smallAngle && !(same(a.fN, b.fN) && same(a.fP, b.fP) && same(a.mN, b.mN) && same(a.mP, b.mP) &&
-                          same(a.pos2, b.pos2) && same(a.a2v, b.a2v) && a.smallAngle == b.smallAngle && a.lvv == b.lvv))
+    if (!(same(a.fN, b.fN) && same(a.fP, b.fP) && same(a.mN, b.mN) && same(a.mP, b.mP) && same(a.pos2, b.pos2) &&
+          same(a.a1v, b.a1v) && same(a.a2v, b.a2v) && a.smallAngle == b.smallAngle && a.lvv == b.lvv))
       bad_forward++;
-    if (!a.smallAngle || c % 4) continue;  // derivative checks on every fourth case
+    if (a.smallAngle != (kind == 0)) continue;  // stayed in the branch its kind aims at
+    if (c % 4 && kind == 0) continue;  // derivative checks on every fourth small-angle case, every large one
     link_cases++;
-    for (int k = 0; k < 18; ++k) {
-      d3 s[6] = {D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0)};
+    if (kind) large_cases++;
+    for (int k = 0; k < 21; ++k) {
+      d3 s[7] = {D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0)};
       (k % 3 == 0 ? s[k / 3].x : k % 3 == 1 ? s[k / 3].y : s[k / 3].z) = 1.0;
       LinkGrad g;
-      if (!link_adjoint(in, s[0], s[1], s[2], s[3], s[4], s[5], g)) continue;
-      // steps large enough that the float-rounded axial strain and stress change by many ulps
+      if (!link_adjoint(in, s[0], s[1], s[2], s[3], s[4], s[5], s[6], g)) continue;
+      // steps large enough that the float-rounded axial strain and stress change by many ulps (a
+      // large-angle link carries a strain of ~0.1-0.6, so its steps are larger; its rotation vectors
+      // and frame formulas have kinks within 1e-4 of a quaternion component)
+      const double hs = kind ? 100.0 : 1.0, hq = kind ? 3.0 : 1.0;
       std::vector<double> fd, ad;
       auto J = [&](const LinkIn& x) { return link_out(link_forward(x), k); };
+      // a large-angle link's difference is taken at six steps (10 h down to h / 30) and the one
+      // nearest the adjoint kept: rounding noise grows as the step shrinks, and the kinks of the
+      // frame and rotation-vector formulas sit within the larger steps of some inputs
       auto dd = [&](double* x, double h, double grad) {
-        double x0 = *x;
-        *x = x0 + h; double jp = J(in);
-        *x = x0 - h; double jm = J(in);
-        *x = x0;
-        fd.push_back((jp - jm) / (2 * h));
+        double x0 = *x, best = 0;
+        const double scales[6] = {1.0, 10.0, 3.0, 1.0 / 3, 0.1, 1.0 / 30};
+        for (int t = 0; t < (kind ? 6 : 1); ++t) {
+          const double hh = h * scales[t];
+          *x = x0 + hh; double jp = J(in);
+          *x = x0 - hh; double jm = J(in);
+          *x = x0;
+          const double d = (jp - jm) / (2 * hh);
+          if (t == 0 || std::fabs(d - grad) < std::fabs(best - grad)) best = d;
+        }
+        fd.push_back(best);
         ad.push_back(grad);
       };
-      dd(&in.pn.x, 1e-7, g.gpn.x); dd(&in.pn.y, 1e-7, g.gpn.y); dd(&in.pn.z, 1e-7, g.gpn.z);
-      dd(&in.pp.x, 1e-7, g.gpp.x); dd(&in.pp.y, 1e-7, g.gpp.y); dd(&in.pp.z, 1e-7, g.gpp.z);
-      dd(&in.qn.w, 1e-5, g.gqn.w); dd(&in.qn.x, 1e-5, g.gqn.x); dd(&in.qn.y, 1e-5, g.gqn.y); dd(&in.qn.z, 1e-5, g.gqn.z);
-      dd(&in.qp.w, 1e-5, g.gqp.w); dd(&in.qp.x, 1e-5, g.gqp.x); dd(&in.qp.y, 1e-5, g.gqp.y); dd(&in.qp.z, 1e-5, g.gqp.z);
-      dd(&in.oldPos2.x, 1e-8, g.gOldPos2.x); dd(&in.oldPos2.y, 1e-8, g.gOldPos2.y); dd(&in.oldPos2.z, 1e-8, g.gOldPos2.z);
-      dd(&in.oldA1.x, 1e-6, g.gOldA1.x); dd(&in.oldA1.y, 1e-6, g.gOldA1.y); dd(&in.oldA1.z, 1e-6, g.gOldA1.z);
-      dd(&in.oldA2.x, 1e-6, g.gOldA2.x); dd(&in.oldA2.y, 1e-6, g.gOldA2.y); dd(&in.oldA2.z, 1e-6, g.gOldA2.z);
-      dd(&in.rest, 1e-7, g.gRest);
+      dd(&in.pn.x, 1e-7 * hs, g.gpn.x); dd(&in.pn.y, 1e-7 * hs, g.gpn.y); dd(&in.pn.z, 1e-7 * hs, g.gpn.z);
+      dd(&in.pp.x, 1e-7 * hs, g.gpp.x); dd(&in.pp.y, 1e-7 * hs, g.gpp.y); dd(&in.pp.z, 1e-7 * hs, g.gpp.z);
+      dd(&in.qn.w, 1e-5 * hq, g.gqn.w); dd(&in.qn.x, 1e-5 * hq, g.gqn.x); dd(&in.qn.y, 1e-5 * hq, g.gqn.y);
+      dd(&in.qn.z, 1e-5 * hq, g.gqn.z);
+      dd(&in.qp.w, 1e-5 * hq, g.gqp.w); dd(&in.qp.x, 1e-5 * hq, g.gqp.x); dd(&in.qp.y, 1e-5 * hq, g.gqp.y);
+      dd(&in.qp.z, 1e-5 * hq, g.gqp.z);
+      dd(&in.oldPos2.x, 1e-8 * hs, g.gOldPos2.x); dd(&in.oldPos2.y, 1e-8 * hs, g.gOldPos2.y);
+      dd(&in.oldPos2.z, 1e-8 * hs, g.gOldPos2.z);
+      dd(&in.oldA1.x, 1e-6 * hq, g.gOldA1.x); dd(&in.oldA1.y, 1e-6 * hq, g.gOldA1.y); dd(&in.oldA1.z, 1e-6 * hq, g.gOldA1.z);
+      dd(&in.oldA2.x, 1e-6 * hq, g.gOldA2.x); dd(&in.oldA2.y, 1e-6 * hq, g.gOldA2.y); dd(&in.oldA2.z, 1e-6 * hq, g.gOldA2.z);
+      dd(&in.rest, 1e-7 * hs, g.gRest);
       {
         float E0 = in.E;
         double h = 1e-3;
@@ -209,12 +257,14 @@ int main() {
         fd.push_back((jp - jm) / (hp + hm));
         ad.push_back(side ? g.gDmP : g.gDmN);
       }
-      cl.tag = k;
-      cl.row(fd, ad);
+      Check& ck = kind ? cll : cl;
+      ck.tag = k;
+      ck.row(fd, ad);
     }
   }
-  printf("link_forward_mismatch %d 200\n", bad_forward);
+  printf("link_forward_mismatch %d 300\n", bad_forward);
   printf("%s %.3e %d %d\n", cl.name, cl.err, cl.n, link_cases);
+  printf("%s %.3e %d %d\n", cll.name, cll.err, cll.n, large_cases);
 
   int bad_vforward = 0, vcases = 0;
   Check cv{"voxel"};

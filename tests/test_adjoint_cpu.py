@@ -1,7 +1,9 @@
 """Host-side check of the hand-written step adjoint (voxelyze_gb300/csrc/vx_adjoint.cuh), compiled
 with g++: its forward recomputation matches vx64::link_update / vx64::voxel_update bit for bit on
 random inputs, and its derivatives match central differences of that forward output by output
-(worst relative error, floored at 1e-4 of each output's largest gradient component, below 2e-3)."""
+(worst relative error, floored at 1e-4 of each output's largest gradient component, below 2e-3).
+Large-angle links (both frame formulas of orientLink, strains of 0.1-0.6): the difference nearest
+the adjoint among six steps, floored at 1e-3 of each output's largest component, below 5e-3."""
 from __future__ import annotations
 
 import os
@@ -26,4 +28,5 @@ def test_adjoint_against_finite_differences_on_cpu(tmp_path):
     assert res["link_forward_mismatch"][0] == 0
     assert res["voxel_forward_mismatch"][0] == 0
     assert res["link"][1] > 10000 and res["link"][0] < 2e-3
+    assert res["link_large"][2] >= 100 and res["link_large"][0] < 5e-3
     assert res["voxel"][1] > 10000 and res["voxel"][0] < 2e-3

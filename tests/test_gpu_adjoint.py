@@ -140,6 +140,65 @@ def test_adjoint_with_partial_fixes(product_lib):
         assert two <= 1e-4 and inf <= 1e-4
 
 
+def _beams(n=8, length=12, E_range=(1e4, 3e4), seed=7, tip=-0.05):
+    """n soft cantilevers of length x 2 x 2 cells (one material per voxel, E log-uniform in E_range,
+    density 1000, CTE 0.01), fixed at x = 0, each of the four tip voxels pulled down by `tip` N,
+    gravity, no floor; per-voxel phases.  They bend far enough for links near the root to take
+    orientLink's large-angle branch."""
+    rng = np.random.default_rng(seed)
+    xyz, body = [], []
+    for b in range(n):
+        for x in range(length):
+            for y in range(2):
+                for z in range(2):
+                    xyz.append((x, 4 * b + y, 20 + z))
+                    body.append(b)
+    xyz = np.array(xyz, np.int32)
+    nv = len(xyz)
+    lo, hi = np.log10(E_range[0]), np.log10(E_range[1])
+    mats = [S.Material(E=float(e), rho=1e3, cte=0.01) for e in (10.0 ** rng.uniform(lo, hi, nv)).astype(np.float32)]
+    sc = S.Scene(0.01, mats, np.arange(nv, dtype=np.int32), xyz, gravity=1.0, floor=False,
+                 body=np.array(body, np.int32), name="beams")
+    sc.fixed_all = np.flatnonzero(xyz[:, 0] == 0)
+    sc.force_idx = np.flatnonzero(xyz[:, 0] == length - 1)
+    sc.force_val = np.tile(np.array([[0.0, 0.0, tip]], np.float32), (len(sc.force_idx), 1))
+    sc.phase = rng.uniform(0.0, 2.0 * np.pi, nv).astype(np.float32)
+    return sc
+
+
+def test_adjoint_through_large_angle_links(product_lib):
+    """Soft cantilevers pulled at the tip bend until links near the root take orientLink's
+    large-angle branch (VX_Link.cpp:77-119: the frame from FromAngleToPosX, the angle1 rotation of
+    the negative end's forces).  The adjoint differentiates both branches.  Central differences
+    over 200 steps (no floor, so no contact decisions) at steps of 4e-3 relative (E, density) and
+    0.04 rad (phase) and a quarter of each: where a perturbed run moves a link's switch between the
+    branches to another step the two differences disagree, and such parameters are reported and
+    left out; every other parameter, of every kind, agrees with the adjoint to 1e-3 after Richardson
+    extrapolation."""
+    sc = _beams()
+    off = G.body_offsets(sc)
+    sim, _ = G.build(product_lib, sc, sc.phase, AMP, FREQ)
+    dt = sim.recommended_time_step()
+    assert sim.do_time_steps(200, dt) == 200
+    large = int(np.count_nonzero(sim.link_state()["smallAngle"] == 0))
+    print(f"links in the large-angle branch after 200 steps: {large} of {sim.link_count()}")
+    assert large > 0
+    rng = np.random.default_rng(3)
+    kinds = ["E", "rho", "phase"]
+    free = lambda b: [v for v in range(off[b], off[b + 1]) if sc.xyz[v, 0] > 0]
+    pick = [(b, int(rng.choice(free(b))), kinds[b % 3]) for b in range(len(off) - 1)]
+    rows, _, _, _ = G.check(product_lib, sc, 200, 50, pick, 4e-3, 0.04, AMP, FREQ, frozen=True)
+    err = np.array([r["richardson_error"] for r in rows])
+    for (b, v, kind), r in zip(pick, rows):
+        print("body %3d voxel %5d d/d%-5s adjoint % .6e D(h) % .6e D(h/4) % .6e extrapolated % .6e error %.2e"
+              % (b, v, kind, r["adjoint"], r["fd_h"], r["fd_h4"], r["richardson"], r["richardson_error"]))
+    print(f"large-angle beams: error median {np.median(err):.2e}, max {err.max():.2e}")
+    smooth = [abs(r["fd_h"] - r["fd_h4"]) <= 1e-2 * max(abs(r["fd_h"]), abs(r["fd_h4"])) for r in rows]
+    print(f"{sum(smooth)} of {len(rows)} parameters with agreeing differences")
+    assert sum(smooth) >= 6 and {k for (b, v, k), s in zip(pick, smooth) if s} == set(kinds)
+    assert max(e for e, s in zip(err, smooth) if s) <= 1e-3
+
+
 def test_decision_replay_follows_the_recorded_branches(product_lib):
     """Replaying a run's own decisions reproduces it bit for bit; a perturbed scene, left to decide
     for itself, takes other branches (which replay holds to the recorded ones)."""

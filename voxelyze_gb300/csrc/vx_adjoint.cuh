@@ -1,8 +1,9 @@
 // Reverse-mode derivatives of one FP64 time step (link pass + voxel pass), hand-written.
 //
 // Scope of the differentiated step: linear link materials with Poisson's ratio 0 and no failure
-// strain, links in the small-angle branch (VX_Link.cpp:96-103), no voxel-voxel collisions; externals
-// add forces and moments and fix any of the six degrees of freedom; floor contact and
+// strain, no voxel-voxel collisions; links in either branch of orientLink (VX_Link.cpp:77-119, the
+// branch and its hysteresis taken as the forward pass took them); externals add forces and moments
+// and fix any of the six degrees of freedom; floor contact and
 // static/kinetic friction are differentiated along the branch the forward pass took
 // (VX_Voxel.cpp:274-298 and the latch at :194-205).  Every forward quantity is recomputed here with
 // the arithmetic of vx_phys64.cuh from the state recorded at the start of the step; the derivative
@@ -188,6 +189,77 @@ struct LinkOut {
   float axial, stress;
 };
 
+// CVX_Link::orientLink's large-angle frame (vx64::from_angle_to_pos_x, Quat3D::FromAngleToPosX,
+// include/Quat3D.h:163-204): the rotation q that takes the link direction r onto +x
+VX_HD void from_angle_to_pos_x(q4& q, const d3& r) {
+  if (r.x == 0 && r.y == 0 && r.z == 0) return;
+  double yx = r.y / r.x, zx = r.z / r.x;
+  if (yx < 1.732e-2 && yx > -1.732e-2 && zx < 1.732e-2 && zx > -1.732e-2) {
+    q.x = 0;
+    q.y = 0.5 * zx;
+    q.z = -0.5 * yx;
+    q.w = 1 + 0.5 * (-q.y * q.y - q.z * q.z);
+    return;
+  }
+  d3 n = r;
+  double l = sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+  if (l > 0) {
+    double li = 1.0 / l;
+    n.x *= li; n.y *= li; n.z *= li;
+  }
+  int f = 0;
+  double theta = vxm::cr_acos(n.x, &f);
+  if (theta > 3.14159265358979 - 1e-7) {
+    q = Q4(0, 0, 1, 0);
+    return;
+  }
+  double ami = 1.0 / sqrt(n.z * n.z + n.y * n.y);
+  double a = 0.5 * theta;
+  double s = vxm::cr_sin(a, &f);
+  q.w = vxm::cr_cos(a, &f);
+  q.x = 0;
+  q.y = n.z * ami * s;
+  q.z = -n.y * ami * s;
+}
+// Its adjoint with respect to r (the starting q is the identity), along the branch r takes; the
+// antiparallel branch is a constant.
+VX_HD void from_angle_to_pos_x_adj(const d3& r, const q4& gq, d3& gr) {
+  if (r.x == 0 && r.y == 0 && r.z == 0) return;
+  double yx = r.y / r.x, zx = r.z / r.x;
+  if (yx < 1.732e-2 && yx > -1.732e-2 && zx < 1.732e-2 && zx > -1.732e-2) {
+    const double qy = 0.5 * zx, qz = -0.5 * yx;
+    const double gqy = gq.y - qy * gq.w, gqz = gq.z - qz * gq.w;  // w = 1 - (qy^2 + qz^2) / 2
+    const double gzx = 0.5 * gqy, gyx = -0.5 * gqz;
+    gr.y += gyx / r.x;
+    gr.z += gzx / r.x;
+    gr.x -= (gyx * r.y + gzx * r.z) / (r.x * r.x);
+    return;
+  }
+  const double l = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+  const d3 n = D3(r.x / l, r.y / l, r.z / l);
+  int f = 0;
+  const double theta = vxm::cr_acos(n.x, &f);
+  if (theta > 3.14159265358979 - 1e-7) return;
+  const double ami = 1.0 / sqrt(n.z * n.z + n.y * n.y);
+  const double a = 0.5 * theta, s = sin(a), c = cos(a);
+  // q = (cos a, 0, u sin a, w sin a) with (u, w) = (n.z, -n.y) ami
+  const double u = n.z * ami, w = -n.y * ami;
+  const double gs = u * gq.y + w * gq.z;
+  const double ga = -s * gq.w + c * gs;
+  const double gu = s * gq.y, gw = s * gq.z;
+  const double gtheta = 0.5 * ga;
+  d3 gn = D3(-gtheta / sqrt(1.0 - n.x * n.x), 0, 0);
+  const double gami = n.z * gu - n.y * gw;
+  const double ami3 = ami * ami * ami;
+  gn.z += ami * gu - n.z * ami3 * gami;
+  gn.y += -ami * gw - n.y * ami3 * gami;
+  // n = r / |r|
+  const double ng = n.x * gn.x + n.y * gn.y + n.z * gn.z;
+  gr.x += (gn.x - n.x * ng) / l;
+  gr.y += (gn.y - n.y * ng) / l;
+  gr.z += (gn.z - n.z * ng) / l;
+}
+
 // CVX_Link::updateForces for a linear, nu = 0, non-failing material (vx64::link_update's arithmetic)
 VX_HD LinkOut link_forward(const LinkIn& in) {
   LinkOut o;
@@ -197,6 +269,7 @@ VX_HD LinkOut link_forward(const LinkIn& in) {
   q4 totalRot = Q4(angle1.w, -angle1.x, -angle1.y, -angle1.z);
   pos2 = vx64::rotate(totalRot, pos2);
   angle2 = vx64::qmul(totalRot, angle2);
+  angle1 = Q4(1, 0, 0, 0);
   bool smallAngle = in.smallAngle, lvv = in.lvv;
   float smallTurn = (float)((fabs(pos2.z) + fabs(pos2.y)) / pos2.x);
   float extendPerc = (float)(fabs(1 - pos2.x / in.rest));
@@ -209,8 +282,14 @@ VX_HD LinkOut link_forward(const LinkIn& in) {
     lvv = false;
   }
   o.smallAngle = smallAngle;
-  pos2.x -= in.rest;  // the large-angle branch is outside the differentiated scope (checked by the caller)
-  d3 a1v = D3(0, 0, 0);
+  if (smallAngle) {
+    pos2.x -= in.rest;
+  } else {
+    from_angle_to_pos_x(angle1, pos2);
+    angle2 = vx64::qmul(angle1, angle2);
+    pos2 = D3(sqrt(pos2.x * pos2.x + pos2.y * pos2.y + pos2.z * pos2.z) - in.rest, 0, 0);
+  }
+  d3 a1v = rotation_vector(angle1);
   d3 a2v = rotation_vector(angle2);
   d3 dPos2 = D3(0.5 * (pos2.x - in.oldPos2.x), 0.5 * (pos2.y - in.oldPos2.y), 0.5 * (pos2.z - in.oldPos2.z));
   d3 dA1 = D3(0.5 * (a1v.x - in.oldA1.x), 0.5 * (a1v.y - in.oldA1.y), 0.5 * (a1v.z - in.oldA1.z));
@@ -238,6 +317,10 @@ VX_HD LinkOut link_forward(const LinkIn& in) {
   } else {
     lvv = true;
   }
+  if (!smallAngle) {
+    fN = vx64::rotate_inv(angle1, fN);
+    mN = vx64::rotate_inv(angle1, mN);
+  }
   fP = vx64::rotate_inv(angle2, fP);
   mP = vx64::rotate_inv(angle2, mP);
   o.fN = vx64::to_axis_original(in.axis, fN);
@@ -260,18 +343,18 @@ struct LinkGrad {
   double gRest, gE, gDmN, gDmP;  // gE: with respect to the link material's E (all constants scale with it)
 };
 
-// Adjoint of link_forward.  gfN..gmP: adjoints of the four force/moment outputs; gPos2, gA2v: of
-// the new link pose (read by the next step's damping terms).  Returns false when the step left the
-// small-angle branch (outside the differentiated scope).
+// Adjoint of link_forward, in both branches of orientLink, along the branch the step takes.
+// gfN..gmP: adjoints of the four force/moment outputs; gPos2, gA1v, gA2v: of the new link pose
+// (read by the next step's damping terms).
 VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, const d3& gmN_o, const d3& gmP_o,
-                        const d3& gPos2_in, const d3& gA2v_in, LinkGrad& g) {
+                        const d3& gPos2_in, const d3& gA1v_in, const d3& gA2v_in, LinkGrad& g) {
   // ---- forward recomputation ----
   d3 D = vx64::to_axis_x(in.axis, D3(in.pp.x - in.pn.x, in.pp.y - in.pn.y, in.pp.z - in.pn.z));
   q4 A1 = vx64::to_axis_x(in.axis, in.qn);
   q4 A2 = vx64::to_axis_x(in.axis, in.qp);
   q4 T = Q4(A1.w, -A1.x, -A1.y, -A1.z);
   d3 R = vx64::rotate(T, D);
-  q4 G = vx64::qmul(T, A2);
+  q4 G0 = vx64::qmul(T, A2);
   bool smallAngle = in.smallAngle, lvv = in.lvv;
   float smallTurn = (float)((fabs(R.z) + fabs(R.y)) / R.x);
   float extendPerc = (float)(fabs(1 - R.x / in.rest));
@@ -283,9 +366,18 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
     smallAngle = false;
     lvv = false;
   }
-  if (!smallAngle) return false;
-  d3 p = D3(R.x - in.rest, R.y, R.z);
-  d3 a1 = D3(0, 0, 0);
+  q4 Q1 = Q4(1, 0, 0, 0), G = G0;
+  d3 p;
+  double Rlen = 0;
+  if (smallAngle) {
+    p = D3(R.x - in.rest, R.y, R.z);
+  } else {
+    from_angle_to_pos_x(Q1, R);
+    G = vx64::qmul(Q1, G0);
+    Rlen = sqrt(R.x * R.x + R.y * R.y + R.z * R.z);
+    p = D3(Rlen - in.rest, 0, 0);
+  }
+  d3 a1 = rotation_vector(Q1);
   d3 a2v = rotation_vector(G);
   d3 dP = D3(0.5 * (p.x - in.oldPos2.x), 0.5 * (p.y - in.oldPos2.y), 0.5 * (p.z - in.oldPos2.z));
   d3 dA1 = D3(0.5 * (a1.x - in.oldA1.x), 0.5 * (a1.y - in.oldA1.y), 0.5 * (a1.z - in.oldA1.z));
@@ -294,7 +386,9 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
   float stress = in.E * (float)axial;
   const double b1 = in.b1, b2 = in.b2, b3 = in.b3, a2c = in.a2;
   d3 fN0 = D3((double)(stress * in.tArea), b1 * p.y - b2 * (a1.z + a2v.z), b1 * p.z + b2 * (a1.y + a2v.y));
+  d3 mN0 = D3(a2c * (a2v.x - a1.x), -b2 * p.z - b3 * (2 * a1.y + a2v.y), b2 * p.y - b3 * (2 * a1.z + a2v.z));
   d3 mP0 = D3(a2c * (a1.x - a2v.x), -b2 * p.z - b3 * (a1.y + 2 * a2v.y), b2 * p.y - b3 * (a1.z + 2 * a2v.z));
+  d3 fN = fN0, mN = mN0;
   d3 fP = D3(-fN0.x, -fN0.y, -fN0.z);
   d3 mP = mP0;
   d3 pc = D3(0, 0, 0), tN = D3(0, 0, 0), tP = D3(0, 0, 0);
@@ -302,22 +396,31 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
   const double dmN = in.dmN, dmP = in.dmP;
   if (lvv) {
     pc = D3(sqA1 * dP.x, sqB1 * dP.y - sqB2 * (dA1.z + dA2.z), sqB1 * dP.z + sqB2 * (dA1.y + dA2.y));
+    fN.x += dmN * pc.x; fN.y += dmN * pc.y; fN.z += dmN * pc.z;
     fP.x -= dmP * pc.x; fP.y -= dmP * pc.y; fP.z -= dmP * pc.z;
     tN = D3(-sqA2 * (dA2.x - dA1.x), sqB2 * dP.z + sqB3 * (2 * dA1.y + dA2.y), -sqB2 * dP.y + sqB3 * (2 * dA1.z + dA2.z));
     tP = D3(sqA2 * (dA2.x - dA1.x), sqB2 * dP.z + sqB3 * (dA1.y + 2 * dA2.y), -sqB2 * dP.y + sqB3 * (dA1.z + 2 * dA2.z));
-    double hP = 0.5 * dmP;
+    double hN = 0.5 * dmN, hP = 0.5 * dmP;
+    mN.x -= hN * tN.x; mN.y -= hN * tN.y; mN.z -= hN * tN.z;
     mP.x -= hP * tP.x; mP.y -= hP * tP.y; mP.z -= hP * tP.z;
   }
 
   // ---- reverse ----
   const int ax = in.axis;
-  d3 gfN = vx64::to_axis_x(ax, gfN_o), gfPr = vx64::to_axis_x(ax, gfP_o);
-  d3 gmN = vx64::to_axis_x(ax, gmN_o), gmPr = vx64::to_axis_x(ax, gmP_o);
-  q4 gG = Q4(0, 0, 0, 0);
-  d3 gfP = D3(0, 0, 0), gmP = D3(0, 0, 0);
+  d3 gfNr = vx64::to_axis_x(ax, gfN_o), gfPr = vx64::to_axis_x(ax, gfP_o);
+  d3 gmNr = vx64::to_axis_x(ax, gmN_o), gmPr = vx64::to_axis_x(ax, gmP_o);
+  q4 gG = Q4(0, 0, 0, 0), gQ1 = Q4(0, 0, 0, 0);
+  d3 gfN = D3(0, 0, 0), gmN = D3(0, 0, 0), gfP = D3(0, 0, 0), gmP = D3(0, 0, 0);
+  if (smallAngle) {
+    gfN = gfNr;
+    gmN = gmNr;
+  } else {  // fN = rotate_inv(Q1, fN'), mN likewise
+    rotate_inv_adj(Q1, fN, gfNr, gQ1, gfN);
+    rotate_inv_adj(Q1, mN, gmNr, gQ1, gmN);
+  }
   rotate_inv_adj(G, fP, gfPr, gG, gfP);
   rotate_inv_adj(G, mP, gmPr, gG, gmP);
-  d3 gp = gPos2_in, ga2 = gA2v_in, gdP = D3(0, 0, 0), gdA1 = D3(0, 0, 0), gdA2 = D3(0, 0, 0);
+  d3 gp = gPos2_in, ga2 = gA2v_in, ga1 = gA1v_in, gdP = D3(0, 0, 0), gdA1 = D3(0, 0, 0), gdA2 = D3(0, 0, 0);
   double gb1 = 0, gb2 = 0, gb3 = 0, ga2c = 0, gsqA1 = 0, gsqA2 = 0, gsqB1 = 0, gsqB2 = 0, gsqB3 = 0;
   g.gDmN = 0;
   g.gDmP = 0;
@@ -349,7 +452,6 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
   }
   // fP0 = -fN0
   gfN0.x -= gfP0.x; gfN0.y -= gfP0.y; gfN0.z -= gfP0.z;
-  d3 ga1 = D3(0, 0, 0);
   // fN0
   double gstress = (double)in.tArea * gfN0.x;
   gp.y += b1 * gfN0.y; ga1.z -= b2 * gfN0.y; ga2.z -= b2 * gfN0.y;
@@ -374,20 +476,31 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
   double gE = axial * gstress;
   gp.x += gaxial / in.rest;
   double grest = -p.x / (in.rest * in.rest) * gaxial;
-  // dP, dA1, dA2 (a1 is the constant 0 here)
+  // dP, dA1, dA2
   gp.x += 0.5 * gdP.x; gp.y += 0.5 * gdP.y; gp.z += 0.5 * gdP.z;
   g.gOldPos2 = scale(-0.5, gdP);
+  ga1.x += 0.5 * gdA1.x; ga1.y += 0.5 * gdA1.y; ga1.z += 0.5 * gdA1.z;
   g.gOldA1 = scale(-0.5, gdA1);
   ga2.x += 0.5 * gdA2.x; ga2.y += 0.5 * gdA2.y; ga2.z += 0.5 * gdA2.z;
   g.gOldA2 = scale(-0.5, gdA2);
-  // a2v = rotation_vector(G)
+  // a2v = rotation_vector(G), a1 = rotation_vector(Q1)
   rotation_vector_adj(G, ga2, gG);
-  // p = R - (rest, 0, 0)
-  d3 gR = gp;
-  grest -= gp.x;
-  // G = T * A2 ; R = rotate(T, D) ; T = conj(A1)
+  q4 gG0 = Q4(0, 0, 0, 0);
+  d3 gR = D3(0, 0, 0);
+  if (smallAngle) {  // p = R - (rest, 0, 0), G = G0, a1 = 0
+    gG0 = gG;
+    gR = gp;
+    grest -= gp.x;
+  } else {  // p = (|R| - rest, 0, 0), G = Q1 G0, Q1 = from_angle_to_pos_x(R)
+    rotation_vector_adj(Q1, ga1, gQ1);
+    qmul_adj(Q1, G0, gG, gQ1, gG0);
+    gR = scale(gp.x / Rlen, R);
+    grest -= gp.x;
+    from_angle_to_pos_x_adj(R, gQ1, gR);
+  }
+  // G0 = T * A2 ; R = rotate(T, D) ; T = conj(A1)
   q4 gT = Q4(0, 0, 0, 0), gA2 = Q4(0, 0, 0, 0);
-  qmul_adj(T, A2, gG, gT, gA2);
+  qmul_adj(T, A2, gG0, gT, gA2);
   d3 gD = D3(0, 0, 0);
   rotate_adj(T, D, gR, gT, gD);
   q4 gA1 = Q4(gT.w, -gT.x, -gT.y, -gT.z);

@@ -42,7 +42,7 @@ struct AdjBuf {
   double* accE;         // nv: dJ/dE of each voxel's material
   double* accRho;       // nv: dJ/drho
   double* accPhase;     // nv: dJ/dphase
-  int* err;             // bit 0: a link left the small-angle branch
+  int* err;             // bit 0: a link's adjoint could not be taken
 };
 
 __device__ __forceinline__ double act_dtemp_dphase(const ActParams& A, int v, float time) {
@@ -136,7 +136,6 @@ __global__ void k_adj_link_forces(View S, AdjBuf T, ActParams A, int slot) {
   if (l >= nl) return;
   vxa::LinkIn in = tape_link_in(S, T, A, slot, l);
   vxa::LinkOut o = vxa::link_forward(in);
-  if (!o.smallAngle) atomicOr(T.err, 1);
   const vx64::d3 F[4] = {o.fN, o.fP, o.mN, o.mP};
   for (int k = 0; k < 4; ++k) {
     T.lforce[(3 * k) * (size_t)nl + l] = F[k].x;
@@ -239,9 +238,10 @@ __global__ void k_adj_link(View S, AdjBuf T, ActParams A, int slot) {
   auto g3 = [&](int base, int v) { return vx64::D3(T.gFM[(size_t)base * nv + v], T.gFM[(size_t)(base + 1) * nv + v], T.gFM[(size_t)(base + 2) * nv + v]); };
   vx64::d3 gfN = g3(0, vn), gfP = g3(0, vp), gmN = g3(3, vn), gmP = g3(3, vp);
   vx64::d3 gPos2 = vx64::D3(T.mu[l], T.mu[nl + l], T.mu[2 * nl + l]);
+  vx64::d3 gA1v = vx64::D3(T.mu[3 * nl + l], T.mu[4 * nl + l], T.mu[5 * nl + l]);
   vx64::d3 gA2v = vx64::D3(T.mu[6 * nl + l], T.mu[7 * nl + l], T.mu[8 * nl + l]);
   vxa::LinkGrad g;
-  if (!vxa::link_adjoint(in, gfN, gfP, gmN, gmP, gPos2, gA2v, g)) {
+  if (!vxa::link_adjoint(in, gfN, gfP, gmN, gmP, gPos2, gA1v, gA2v, g)) {
     atomicOr(T.err, 1);
     for (int c = 0; c < 9; ++c) T.mu[(size_t)c * nl + l] = 0.0;
     for (int c = 0; c < 14; ++c) T.lcon[(size_t)c * nl + l] = 0.0;

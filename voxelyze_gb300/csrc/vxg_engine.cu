@@ -2425,7 +2425,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   if (dphase) VXG_CK(cudaMemcpyAsync(dphase, T.accPhase, sizeof(double) * nv, cudaMemcpyDeviceToHost, e->stream));
   VXG_CK(cudaStreamSynchronize(e->stream));
   VXG_CK(cudaGetLastError());
-  if (err & 1) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: a link left the small-angle branch (outside the differentiated scope)");
+  if (err & 1) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: a link's adjoint could not be taken");
   return VXG_OK;
 }
 
