@@ -380,15 +380,23 @@ def run_ours(args, world, rank, local):
     set_temps = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)(("vx_set_temperatures", lib))
     read_pos = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)(("vx_read_positions_async", lib))
     e2e_steps = max(3, min(args.steps, 50))
-    barrier()
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
+
+    def e2e_step(k):
         if set_temps(h, temps.data_ptr()) != 0:
             raise RuntimeError("vx_set_temperatures failed")
         if lib.vx_do_time_step(h, C.c_float(dt)) != 1:
             raise RuntimeError("e2e step diverged")
         if read_pos(h, pos[k % 2].data_ptr()) != 0:
             raise RuntimeError("vx_read_positions_async failed")
+
+    for k in range(3):  # untimed: the first single step captures its graph, the first read allocates
+        e2e_step(k)
+    if lib.vx_read_wait(h) != 0:
+        raise RuntimeError("vx_read_wait failed")
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        e2e_step(k)
     if lib.vx_read_wait(h) != 0:
         raise RuntimeError("vx_read_wait failed")
     e2e_value, _, _ = aggregate_rate(nv * e2e_steps, time.perf_counter() - t0)
