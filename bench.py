@@ -505,7 +505,8 @@ def run_ours(args, world, rank, local):
 
 
 def run_adjoint(args, world, rank, local):
-    """Config 5: reverse-mode gradient of the per-body centre-of-mass x after 2,000 steps with
+    """The gradient workload (256 bodies of 16^3 cells): reverse-mode gradient of the per-body
+    centre-of-mass x after 2,000 steps with
     respect to every voxel's E, density and actuation phase (FP64 path, checkpoints every 100
     steps), timed; then checked against central differences on 64 random parameters."""
     import voxelyze_gb300 as vg

@@ -1,4 +1,5 @@
-"""Central differences of the config-5 objective taken with the REFERENCE build, as a fixture.
+"""Central differences of the body centre-of-mass objective (the gradient workload's) taken with
+the REFERENCE build, as a fixture.
 
 The objective is a body's mass-weighted centre-of-mass x after `nsteps` steps, with each voxel's
 temperature set before every step to amplitude * sin(2 pi frequency t + phase[v]) through

@@ -58,8 +58,8 @@ def test_adjoint_longer_horizon_more_bodies(product_lib):
     _fd_check(product_lib, sc, nsteps=1000, K=100, rel_step=1e-3, phase_step=1e-2, tol=2e-3, seed=1)
 
 
-def test_adjoint_config5_horizon(product_lib):
-    """Config 5's bodies and horizon on a quarter of its population: 64 bodies of 16^3 cells
+def test_adjoint_gradient_workload_horizon(product_lib):
+    """The gradient workload's bodies and horizon on a quarter of its 256 bodies: 64 bodies of 16^3 cells
     (occupancy 0.7), 2,000 steps with floor, friction and gravity, checkpoints every 100 steps; E
     and phase of one voxel in each of 32 bodies.  Over this horizon contact and friction decisions
     make some differences non-smooth at any usable step, so the bound is on the median distance
@@ -72,7 +72,7 @@ def test_adjoint_config5_horizon(product_lib):
             for i, b in enumerate(bodies)]
     rows, _, t_adj, _ = G.check(product_lib, sc, 2000, 100, pick, 1e-3, 1e-2, AMP, FREQ)
     d = np.array([r["distance"] for r in rows if r["smooth"]])
-    print(f"config-5 horizon, {sc.n_voxels} voxels, 2000 steps: adjoint {t_adj:.1f} s; {len(d)} of "
+    print(f"2,000-step gradient horizon, {sc.n_voxels} voxels: adjoint {t_adj:.1f} s; {len(d)} of "
           f"{len(rows)} smooth; distance median {np.median(d):.2e}, 90th pct {np.percentile(d, 90):.2e}, "
           f"max {d.max():.2e}; within 1e-4: {np.mean(d <= 1e-4):.2f}")
     assert len(d) >= 0.75 * len(rows)

@@ -234,7 +234,7 @@ def test_fused_poisson_cache_matches_prepass(product_lib, edit):
 
 @pytest.mark.parametrize("friction", [False, True])
 def test_collisions_fp32c_tracks_fp64(product_lib, friction):
-    """The porous collision scene (config 3's generator at 20^3) dropped onto the floor with
+    """The porous collision scene (the 64^3 collision body's generator at 20^3) dropped onto the floor with
     collisions on: FP32C against FP64.  Both start from the same lattice, so the first pair list
     is the same set; the contact forces are FP32 in FP32C (offsets from lattice offsets plus
     displacement differences).  Without friction FP32C tracks FP64 closely; with friction the

@@ -99,7 +99,7 @@ def _pairs_at_rebuilds(product_lib, oracle_lib, sc, steps, check_every):
 
 
 def test_porous_full_size_full_horizon(product_lib, oracle_lib):
-    """Config 3 at full size over its 5,000-step horizon: every rebuild (the body falls, its surface
+    """The porous 64^3 collision body at full size over its 5,000-step horizon: every rebuild (the body falls, its surface
     voxels drift past the watch distance, it lands) compared pair for pair, the state every 500."""
     rebuilds, compared, max_pairs, g = _pairs_at_rebuilds(product_lib, oracle_lib, S.porous(64), 5000, 500)
     zmin = float(g.voxel_state()["pos"][:, 2].min())
@@ -108,7 +108,7 @@ def test_porous_full_size_full_horizon(product_lib, oracle_lib):
 
 
 def test_porous_reduced_full_horizon(product_lib, oracle_lib):
-    """The config-3 generator at 32^3 over the full 5,000-step horizon: the drop, the impact and the
+    """The porous collision generator at 32^3 over the full 5,000-step horizon: the drop, the impact and the
     contacts; pair lists at every rebuild and the state every 500 steps."""
     rebuilds, compared, max_pairs, g = _pairs_at_rebuilds(product_lib, oracle_lib, S.porous(32), 5000, 500)
     zmin = float(g.voxel_state()["pos"][:, 2].min())
@@ -124,7 +124,7 @@ def _cr_sin(lib, x: float) -> float:
 
 
 def test_population_sample_full_horizon(product_lib, oracle_lib):
-    """The first 64 bodies of the config-4 population, 10,000 steps with the ambient temperature
+    """The first 64 bodies of the 4,096-body population, 10,000 steps with the ambient temperature
     0.1 sin(2 pi 2 t) set before every step (the GPU applies it inside the step)."""
     sc = S.population(64)
     oracle_lib.vxo_set_math(1)
@@ -147,7 +147,7 @@ def test_population_sample_full_horizon(product_lib, oracle_lib):
 
 
 def test_cantilever_error_against_c_library(product_lib, oracle_lib):
-    """Config 1 against the reference's own arithmetic (C-library sin/cos/acos): the error at 1,000
+    """The 40x8x8 cantilever against the reference's own arithmetic (C-library sin/cos/acos): the error at 1,000
     and 10,000 steps, reported (the GPU is bit-identical to the correctly rounded oracle over the
     whole horizon, test_gpu_parity.py)."""
     oracle_lib.vxo_set_math(0)
