@@ -68,6 +68,15 @@ static LinkIn random_link(int kind = 0) {
   in.oldA2 = D3(U(-1e-2, 1e-2), U(-1e-2, 1e-2), U(-1e-2, 1e-2));
   in.rest = L0 * (1 + U(-1e-3, 1e-3));
   in.smallAngle = true;
+  // one link in four has a failure strain: half of them failed already (largest strain so far
+  // 2e-3 against 1e-3), half far from failing
+  in.maxStrain = 0.0f;
+  in.epsilonFail = -1.0f;
+  if (rng() % 4 == 0) {
+    const bool failed = rng() % 2;
+    in.maxStrain = failed ? 2e-3f : 0.0f;
+    in.epsilonFail = failed ? 1e-3f : 0.9f;
+  }
   if (kind) {
     // kind 2: bent, the positive end displaced sideways by 0.2-0.5 of the length (the bend far past
     // the hysteresis bound 1.2 x 0.05); kind 1: stretched by 60 % (past the extension bound 0.5)
@@ -107,14 +116,14 @@ static LinkOut engine_link(const LinkIn& in) {
   double pos2[3] = {in.oldPos2.x, in.oldPos2.y, in.oldPos2.z}, a1v[3] = {in.oldA1.x, in.oldA1.y, in.oldA1.z},
          a2v[3] = {in.oldA2.x, in.oldA2.y, in.oldA2.z};
   double fN[3], fP[3], mN[3], mP[3], rest[1] = {in.rest};
-  float strain[1] = {0}, maxStrain[1] = {0}, strainOffset[1] = {0}, stress[1] = {0}, ratio[1] = {1},
+  float strain[1] = {0}, maxStrain[1] = {in.maxStrain}, strainOffset[1] = {0}, stress[1] = {0}, ratio[1] = {1},
         tArea[1] = {in.tArea}, tSS[1] = {0}, temp[2] = {0, 0}, pStrain[6] = {0}, prevDt[2];
   uint32_t lflags[1] = {(uint32_t)(in.axis << 8) | (in.smallAngle ? VXG_LF_SMALL_ANGLE : 0u) |
                         (in.lvv ? VXG_LF_LOCAL_VEL_VALID : 0u)};
   int lvox[2] = {0, 1}, lmat[1] = {0}, vmat[2] = {0, 1};
   vxg_link_material lm;
   std::memset(&lm, 0, sizeof(lm));
-  lm.linear = 1; lm.ndata = 2; lm.E = in.E; lm.nu = 0; lm.epsilonFail = -1.0f;
+  lm.linear = 1; lm.ndata = 2; lm.E = in.E; lm.nu = 0; lm.epsilonFail = in.epsilonFail;
   lm.a2 = in.a2; lm.b1 = in.b1; lm.b2 = in.b2; lm.b3 = in.b3;
   lm.sqA1 = in.sqA1; lm.sqA2xIp = in.sqA2xIp; lm.sqB1 = in.sqB1; lm.sqB2xFMp = in.sqB2xFMp; lm.sqB3xIp = in.sqB3xIp;
   lm.strain[1] = 1e30f;

@@ -140,11 +140,12 @@ def test_adjoint_with_partial_fixes(product_lib):
         assert two <= 1e-4 and inf <= 1e-4
 
 
-def _beams(n=8, length=12, E_range=(1e4, 3e4), seed=7, tip=-0.05):
+def _beams(n=8, length=12, E_range=(1e4, 3e4), seed=7, tip=-0.05, fail_strain=None):
     """n soft cantilevers of length x 2 x 2 cells (one material per voxel, E log-uniform in E_range,
     density 1000, CTE 0.01), fixed at x = 0, each of the four tip voxels pulled down by `tip` N,
     gravity, no floor; per-voxel phases.  They bend far enough for links near the root to take
-    orientLink's large-angle branch."""
+    orientLink's large-angle branch.  fail_strain: a linear material with that failure strain
+    (CVX_Material::setModelLinear's failure stress over E)."""
     rng = np.random.default_rng(seed)
     xyz, body = [], []
     for b in range(n):
@@ -156,7 +157,9 @@ def _beams(n=8, length=12, E_range=(1e4, 3e4), seed=7, tip=-0.05):
     xyz = np.array(xyz, np.int32)
     nv = len(xyz)
     lo, hi = np.log10(E_range[0]), np.log10(E_range[1])
-    mats = [S.Material(E=float(e), rho=1e3, cte=0.01) for e in (10.0 ** rng.uniform(lo, hi, nv)).astype(np.float32)]
+    Es = (10.0 ** rng.uniform(lo, hi, nv)).astype(np.float32)
+    mats = [S.Material(E=float(e), rho=1e3, cte=0.01,
+                       model=None if fail_strain is None else ("linear", float(e), float(e) * fail_strain)) for e in Es]
     sc = S.Scene(0.01, mats, np.arange(nv, dtype=np.int32), xyz, gravity=1.0, floor=False,
                  body=np.array(body, np.int32), name="beams")
     sc.fixed_all = np.flatnonzero(xyz[:, 0] == 0)
@@ -196,6 +199,35 @@ def test_adjoint_through_large_angle_links(product_lib):
     smooth = [abs(r["fd_h"] - r["fd_h4"]) <= 1e-2 * max(abs(r["fd_h"]), abs(r["fd_h4"])) for r in rows]
     print(f"{sum(smooth)} of {len(rows)} parameters with agreeing differences")
     assert sum(smooth) >= 6 and {k for (b, v, k), s in zip(pick, smooth) if s} == set(kinds)
+    assert max(e for e, s in zip(err, smooth) if s) <= 1e-3
+
+
+def test_adjoint_through_failing_links(product_lib):
+    """Linear materials with a failure strain (CVX_Link::isFailed: once a link's largest strain
+    passes it, it applies no force): the bending cantilevers with a failure strain of 0.05, so that
+    links near the roots fail during the 200 steps.  The adjoint follows each link's failure as the
+    forward run took it (the taped largest strain); central differences as for the large-angle
+    test, with parameters whose perturbed runs fail a link at another step reported and left out."""
+    sc = _beams(fail_strain=0.05)
+    off = G.body_offsets(sc)
+    sim, _ = G.build(product_lib, sc, sc.phase, AMP, FREQ)
+    dt = sim.recommended_time_step()
+    assert sim.do_time_steps(200, dt) == 200
+    failed = int(np.count_nonzero(sim.link_state()["maxStrain"] > 0.05))
+    print(f"failed links after 200 steps: {failed} of {sim.link_count()}")
+    assert failed > 0
+    rng = np.random.default_rng(4)
+    kinds = ["E", "rho", "phase"]
+    free = lambda b: [v for v in range(off[b], off[b + 1]) if sc.xyz[v, 0] > 0]
+    pick = [(b, int(rng.choice(free(b))), kinds[b % 3]) for b in range(len(off) - 1)]
+    rows, _, _, _ = G.check(product_lib, sc, 200, 50, pick, 4e-3, 0.04, AMP, FREQ, frozen=True)
+    err = np.array([r["richardson_error"] for r in rows])
+    for (b, v, kind), r in zip(pick, rows):
+        print("body %3d voxel %5d d/d%-5s adjoint % .6e D(h) % .6e D(h/4) % .6e extrapolated % .6e error %.2e"
+              % (b, v, kind, r["adjoint"], r["fd_h"], r["fd_h4"], r["richardson"], r["richardson_error"]))
+    smooth = [abs(r["fd_h"] - r["fd_h4"]) <= 1e-2 * max(abs(r["fd_h"]), abs(r["fd_h4"])) for r in rows]
+    print(f"{sum(smooth)} of {len(rows)} parameters with agreeing differences")
+    assert sum(smooth) >= 5 and {k for (b, v, k), s in zip(pick, smooth) if s} == set(kinds)
     assert max(e for e, s in zip(err, smooth) if s) <= 1e-3
 
 

@@ -181,13 +181,23 @@ struct LinkIn {
   bool smallAngle, lvv;  // flags at the start of the step
   float E, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp, tArea;
   float dmN, dmP;        // damping multipliers 2 sqrt(m) zeta / previous dt of the two voxels
+  float maxStrain;       // the largest axial strain so far (CVX_Link::maxStrain) at the step's start
+  float epsilonFail;     // the material's failure strain, -1: none
 };
 struct LinkOut {
   d3 fN, fP, mN, mP;     // in the voxels' frames, original axes (what the voxel pass gathers)
   d3 pos2, a1v, a2v;
-  bool smallAngle, lvv;
-  float axial, stress;
+  bool smallAngle, lvv, failed;
+  float axial, stress, maxStrain;
 };
+// CVX_Link::updateStrain's history for a linear material and CVX_Link::isFailed
+// (VX_Link.cpp:220-249, 149-217): the largest strain so far, and whether it passed the failure strain
+VX_HD bool link_failed(const LinkIn& in, float axial, float* maxStrain) {
+  float ms = in.maxStrain;
+  if (axial > ms) ms = axial;
+  *maxStrain = ms;
+  return in.epsilonFail != -1.0f && ms > in.epsilonFail;
+}
 
 // CVX_Link::orientLink's large-angle frame (vx64::from_angle_to_pos_x, Quat3D::FromAngleToPosX,
 // include/Quat3D.h:163-204): the rotation q that takes the link direction r onto +x
@@ -282,6 +292,7 @@ VX_HD LinkOut link_forward(const LinkIn& in) {
     lvv = false;
   }
   o.smallAngle = smallAngle;
+  const bool lvvBranch = lvv;  // the flag after the branch test, before the force terms set it
   if (smallAngle) {
     pos2.x -= in.rest;
   } else {
@@ -296,6 +307,7 @@ VX_HD LinkOut link_forward(const LinkIn& in) {
   d3 dA2 = D3(0.5 * (a2v.x - in.oldA2.x), 0.5 * (a2v.y - in.oldA2.y), 0.5 * (a2v.z - in.oldA2.z));
   float axial = (float)(pos2.x / in.rest);
   float stress = in.E * axial;
+  o.failed = link_failed(in, axial, &o.maxStrain);
   float b1 = in.b1, b2 = in.b2, b3 = in.b3, a2 = in.a2;
   d3 fN = D3((double)(stress * in.tArea), b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
   d3 fP = D3(-fN.x, -fN.y, -fN.z);
@@ -327,6 +339,10 @@ VX_HD LinkOut link_forward(const LinkIn& in) {
   o.fP = vx64::to_axis_original(in.axis, fP);
   o.mN = vx64::to_axis_original(in.axis, mN);
   o.mP = vx64::to_axis_original(in.axis, mP);
+  if (o.failed) {  // a failed link applies nothing; the force terms that set the flag do not run
+    o.fN = o.fP = o.mN = o.mP = D3(0, 0, 0);
+    lvv = lvvBranch;
+  }
   o.pos2 = pos2;
   o.a1v = a1v;
   o.a2v = a2v;
@@ -407,8 +423,11 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
 
   // ---- reverse ----
   const int ax = in.axis;
-  d3 gfNr = vx64::to_axis_x(ax, gfN_o), gfPr = vx64::to_axis_x(ax, gfP_o);
-  d3 gmNr = vx64::to_axis_x(ax, gmN_o), gmPr = vx64::to_axis_x(ax, gmP_o);
+  float msNew;
+  const bool failed = link_failed(in, (float)axial, &msNew);  // its forces depend on nothing
+  const d3 zero = D3(0, 0, 0);
+  d3 gfNr = vx64::to_axis_x(ax, failed ? zero : gfN_o), gfPr = vx64::to_axis_x(ax, failed ? zero : gfP_o);
+  d3 gmNr = vx64::to_axis_x(ax, failed ? zero : gmN_o), gmPr = vx64::to_axis_x(ax, failed ? zero : gmP_o);
   q4 gG = Q4(0, 0, 0, 0), gQ1 = Q4(0, 0, 0, 0);
   d3 gfN = D3(0, 0, 0), gmN = D3(0, 0, 0), gfP = D3(0, 0, 0), gmP = D3(0, 0, 0);
   if (smallAngle) {

@@ -29,6 +29,7 @@ struct AdjBuf {
   float* tpd;           // K x nv previous dt
   double* tl;           // K x 9 nl: pos2 3, angle1v 3, angle2v 3
   uint32_t* tlf;        // K x nl link flags
+  float* tms;           // K x nl largest axial strain so far (failure)
   float* ttime;         // K step start times
   float* ttemp;         // K x nv temperatures each step used (after its actuation)
   double* tforce;       // K x 12 nl link forces and moments of each step (null: recomputed)
@@ -90,6 +91,7 @@ __global__ void k_tape_save(View S, AdjBuf T, int slot) {
       tl[(6 + c) * nl + i] = S.a2v[c * nl + i];
     }
     T.tlf[(size_t)slot * nl + i] = S.lflags[i];
+    T.tms[(size_t)slot * nl + i] = S.maxStrain[i];
   }
   if (i == 0) T.ttime[slot] = S.ctl->time;
 }
@@ -124,6 +126,8 @@ __device__ vxa::LinkIn tape_link_in(const View& S, const AdjBuf& T, const ActPar
   in.E = m.E; in.a2 = m.a2; in.b1 = m.b1; in.b2 = m.b2; in.b3 = m.b3;
   in.sqA1 = m.sqA1; in.sqA2xIp = m.sqA2xIp; in.sqB1 = m.sqB1; in.sqB2xFMp = m.sqB2xFMp; in.sqB3xIp = m.sqB3xIp;
   in.tArea = S.tArea[l];
+  in.maxStrain = T.tms[(size_t)slot * nl + l];
+  in.epsilonFail = m.epsilonFail;
   // CVX_Voxel::dampingMultiplier with the previous dt the step saw (VX_Voxel.h:130)
   in.dmN = 2 * mn.sqrtMass * mn.zetaInternal / T.tpd[(size_t)slot * nv + vn];
   in.dmP = 2 * mp.sqrtMass * mp.zetaInternal / T.tpd[(size_t)slot * nv + vp];

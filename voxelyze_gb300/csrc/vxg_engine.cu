@@ -1598,8 +1598,8 @@ int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const 
     if (vm[k].nu != 0.0f) e->tab_poisson = true;
   e->adj_scope = nullptr;
   for (int k = 0; k < n_lm && !e->adj_scope; ++k)
-    if (!lm[k].linear || lm[k].nu != 0.0f || lm[k].epsilonFail != -1.0f)
-      e->adj_scope = "a link material is not linear, has Poisson's ratio != 0 or a failure strain";
+    if (!lm[k].linear || lm[k].nu != 0.0f)
+      e->adj_scope = "a link material is not linear or has Poisson's ratio != 0";
   for (int k = 0; k < n_vm && !e->adj_scope; ++k)
     if (vm[k].nu != 0.0f) e->adj_scope = "a voxel material has Poisson's ratio != 0";
   VXG_CK(cudaStreamSynchronize(e->stream));
@@ -2334,7 +2334,8 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   auto carve = [&](size_t bytes) { size_t o = (sz + 255) & ~(size_t)255; sz = o + bytes; return o; };
   size_t o_tv = carve(sizeof(double) * 13 * (size_t)nv * K), o_tvf = carve(sizeof(uint32_t) * (size_t)nv * K),
          o_tpd = carve(sizeof(float) * (size_t)nv * K), o_tl = carve(sizeof(double) * 9 * (size_t)nl * K),
-         o_tlf = carve(sizeof(uint32_t) * (size_t)nl * K), o_tt = carve(sizeof(float) * K),
+         o_tlf = carve(sizeof(uint32_t) * (size_t)nl * K), o_tms = carve(sizeof(float) * (size_t)nl * K),
+         o_tt = carve(sizeof(float) * K),
          o_ttemp = carve(sizeof(float) * (size_t)nv * K),
          o_lam = carve(sizeof(double) * 13 * (size_t)nv), o_gfm = carve(sizeof(double) * 6 * (size_t)nv),
          o_mu = carve(sizeof(double) * 9 * (size_t)nl), o_lcon = carve(sizeof(double) * 14 * (size_t)nl),
@@ -2359,6 +2360,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   T.K = K;
   T.tv = (double*)(buf + o_tv); T.tvf = (uint32_t*)(buf + o_tvf); T.tpd = (float*)(buf + o_tpd);
   T.tl = (double*)(buf + o_tl); T.tlf = (uint32_t*)(buf + o_tlf); T.ttime = (float*)(buf + o_tt);
+  T.tms = (float*)(buf + o_tms);
   T.ttemp = (float*)(buf + o_ttemp);
   T.tforce = o_tf ? (double*)(buf + o_tf) : nullptr;
   T.lam = (double*)(buf + o_lam); T.gFM = (double*)(buf + o_gfm); T.mu = (double*)(buf + o_mu);

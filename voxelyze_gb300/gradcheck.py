@@ -62,8 +62,11 @@ def central_differences(lib, scene, pick, nsteps, dt, off, rel_step, phase_step,
         realized = []
         for _, v, kind in pick:
             if kind == "E":
-                s2.materials[v].E = float(np.float32(scene.materials[v].E * (1 + sign * rel_step)))
-                realized.append(s2.materials[v].E)
+                m = s2.materials[v]
+                m.E = float(np.float32(scene.materials[v].E * (1 + sign * rel_step)))
+                if m.model is not None and m.model[0] == "linear":  # setModelLinear(E, failure stress)
+                    m.model = ("linear", m.E) + tuple(m.model[2:])
+                realized.append(m.E)
             elif kind == "rho":
                 s2.materials[v].rho = float(np.float32(scene.materials[v].rho * (1 + sign * rel_step)))
                 realized.append(s2.materials[v].rho)
