@@ -276,11 +276,11 @@ int vxg_autotune(vxg_engine* e, int trial_steps, float dt, int* best_link, int* 
  * with one material per voxel they are the derivatives with respect to that material's E and rho.
  * Reverse mode with hand-written adjoint kernels; the state is checkpointed every checkpoint_every
  * steps and each segment is recomputed once, so device memory grows with checkpoint_every.
- * Scope: linear materials (with or without a failure strain) with Poisson's ratio 0, no
- * collisions; links in either branch of CVX_Link::orientLink; externals may fix any of the degrees
- * of freedom (a partial rotation fix is differentiated through the rotation vector it zeroes);
- * floor contact, friction, each link's branch and its failure are differentiated along the branch
- * the forward run took. */
+ * Scope: linear materials (with or without a failure strain), one Poisson's ratio for every
+ * voxel material (0 or not), no collisions; links in either branch of CVX_Link::orientLink;
+ * externals may fix any of the degrees of freedom (a partial rotation fix is differentiated through
+ * the rotation vector it zeroes); floor contact, friction, each link's branch and its failure are
+ * differentiated along the branch the forward run took. */
 int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every, const int* body_offsets,
                       int n_bodies, double* objective, double* dE, double* drho, double* dphase);
 /* Full device-side copies of the simulation state (checkpoint / restart). */

@@ -72,6 +72,18 @@ static LinkIn random_link(int kind = 0) {
   // 2e-3 against 1e-3), half far from failing
   in.maxStrain = 0.0f;
   in.epsilonFail = -1.0f;
+  // one link in three (with either kind) has Poisson's ratio 0.3 with its ends' Poisson strains
+  in.nu = 0.0f;
+  in.eHat = 0.0f;
+  in.sizeN = in.sizeP = (float)L0;
+  in.nuN = in.nuP = false;
+  in.psn = in.psp = D3(0, 0, 0);
+  if (rng() % 3 == 0) {
+    in.nu = 0.3f;
+    in.nuN = in.nuP = true;
+    in.psn = D3((float)U(-1e-3, 1e-3), (float)U(-1e-3, 1e-3), (float)U(-1e-3, 1e-3));
+    in.psp = D3((float)U(-1e-3, 1e-3), (float)U(-1e-3, 1e-3), (float)U(-1e-3, 1e-3));
+  }
   if (rng() % 4 == 0) {
     const bool failed = rng() % 2;
     in.maxStrain = failed ? 2e-3f : 0.0f;
@@ -101,6 +113,7 @@ static LinkIn random_link(int kind = 0) {
   }
   in.lvv = rng() % 4 != 0;
   set_consts(in, link_consts((float)std::exp(U(std::log(3e5), std::log(3e6))), (float)L0));
+  in.eHat = in.E / ((1 - 2 * in.nu) * (1 + in.nu));
   in.tArea = (float)(L0 * L0);
   double m = 1000.0 * L0 * L0 * L0;
   float dt = 2e-5f;
@@ -117,13 +130,15 @@ static LinkOut engine_link(const LinkIn& in) {
          a2v[3] = {in.oldA2.x, in.oldA2.y, in.oldA2.z};
   double fN[3], fP[3], mN[3], mP[3], rest[1] = {in.rest};
   float strain[1] = {0}, maxStrain[1] = {in.maxStrain}, strainOffset[1] = {0}, stress[1] = {0}, ratio[1] = {1},
-        tArea[1] = {in.tArea}, tSS[1] = {0}, temp[2] = {0, 0}, pStrain[6] = {0}, prevDt[2];
+        tArea[1] = {in.tArea}, tSS[1] = {0}, temp[2] = {0, 0}, prevDt[2];
+  float pStrain[6] = {(float)in.psn.x, (float)in.psp.x, (float)in.psn.y, (float)in.psp.y, (float)in.psn.z,
+                      (float)in.psp.z};
   uint32_t lflags[1] = {(uint32_t)(in.axis << 8) | (in.smallAngle ? VXG_LF_SMALL_ANGLE : 0u) |
                         (in.lvv ? VXG_LF_LOCAL_VEL_VALID : 0u)};
   int lvox[2] = {0, 1}, lmat[1] = {0}, vmat[2] = {0, 1};
   vxg_link_material lm;
   std::memset(&lm, 0, sizeof(lm));
-  lm.linear = 1; lm.ndata = 2; lm.E = in.E; lm.nu = 0; lm.epsilonFail = in.epsilonFail;
+  lm.linear = 1; lm.ndata = 2; lm.E = in.E; lm.nu = in.nu; lm.eHat = in.eHat; lm.epsilonFail = in.epsilonFail;
   lm.a2 = in.a2; lm.b1 = in.b1; lm.b2 = in.b2; lm.b3 = in.b3;
   lm.sqA1 = in.sqA1; lm.sqA2xIp = in.sqA2xIp; lm.sqB1 = in.sqB1; lm.sqB2xFMp = in.sqB2xFMp; lm.sqB3xIp = in.sqB3xIp;
   lm.strain[1] = 1e30f;
@@ -132,6 +147,8 @@ static LinkOut engine_link(const LinkIn& in) {
   // damping_multiplier = 2 sqrtMass zetaInternal / prevDt: choose values that reproduce dmN, dmP
   vm[0].sqrtMass = in.dmN / 2.0f; vm[0].zetaInternal = 1.0f; prevDt[0] = 1.0f;
   vm[1].sqrtMass = in.dmP / 2.0f; vm[1].zetaInternal = 1.0f; prevDt[1] = 1.0f;
+  vm[0].nu = in.nuN ? 0.3f : 0.0f; vm[0].nomSize = in.sizeN;
+  vm[1].nu = in.nuP ? 0.3f : 0.0f; vm[1].nomSize = in.sizeP;
   vx64::Ctl ctl;
   std::memset(&ctl, 0, sizeof(ctl));
   vx64::View S;
@@ -180,6 +197,7 @@ struct Check {
 };
 
 static double link_out(const LinkOut& o, int k) {
+  if (k == 21) return o.axial;
   const d3 O[7] = {o.fN, o.fP, o.mN, o.mP, o.pos2, o.a1v, o.a2v};
   const double v[3] = {O[k / 3].x, O[k / 3].y, O[k / 3].z};
   return v[k % 3];
@@ -209,11 +227,11 @@ int main() {
     if (c % 4 && kind == 0) continue;  // derivative checks on every fourth small-angle case, every large one
     link_cases++;
     if (kind) large_cases++;
-    for (int k = 0; k < 21; ++k) {
+    for (int k = 0; k < 22; ++k) {  // the 21 pose, force and moment components, then the axial strain
       d3 s[7] = {D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0), D3(0, 0, 0)};
-      (k % 3 == 0 ? s[k / 3].x : k % 3 == 1 ? s[k / 3].y : s[k / 3].z) = 1.0;
+      if (k < 21) (k % 3 == 0 ? s[k / 3].x : k % 3 == 1 ? s[k / 3].y : s[k / 3].z) = 1.0;
       LinkGrad g;
-      if (!link_adjoint(in, s[0], s[1], s[2], s[3], s[4], s[5], s[6], g)) continue;
+      if (!link_adjoint(in, s[0], s[1], s[2], s[3], s[4], s[5], s[6], k == 21 ? 1.0 : 0.0, g)) continue;
       // steps large enough that the float-rounded axial strain and stress change by many ulps (a
       // large-angle link carries a strain of ~0.1-0.6, so its steps are larger; its rotation vectors
       // and frame formulas have kinks within 1e-4 of a quaternion component)
@@ -248,6 +266,10 @@ int main() {
       dd(&in.oldA1.x, 1e-6 * hq, g.gOldA1.x); dd(&in.oldA1.y, 1e-6 * hq, g.gOldA1.y); dd(&in.oldA1.z, 1e-6 * hq, g.gOldA1.z);
       dd(&in.oldA2.x, 1e-6 * hq, g.gOldA2.x); dd(&in.oldA2.y, 1e-6 * hq, g.gOldA2.y); dd(&in.oldA2.z, 1e-6 * hq, g.gOldA2.z);
       dd(&in.rest, 1e-7 * hs, g.gRest);
+      if (in.nu != 0.0f) {  // the ends' Poisson strains (floats, so steps of many ulps)
+        dd(&in.psn.x, 1e-4, g.gpsn.x); dd(&in.psn.y, 1e-4, g.gpsn.y); dd(&in.psn.z, 1e-4, g.gpsn.z);
+        dd(&in.psp.x, 1e-4, g.gpsp.x); dd(&in.psp.y, 1e-4, g.gpsp.y); dd(&in.psp.z, 1e-4, g.gpsp.z);
+      }
       {
         float E0 = in.E;
         double h = 1e-3;
@@ -401,5 +423,66 @@ int main() {
   }
   printf("voxel_forward_mismatch %d 400\n", bad_vforward);
   printf("%s %.3e %d %d\n", cv.name, cv.err, cv.n, vcases);
+
+  // the Poisson strains of a voxel (vx64::poisson_strain_links on a one-voxel View whose six slots
+  // hold links 0..5, some absent) against poisson_adjoint, per slot strain
+  Check cp{"poisson"};
+  int pcases = 0;
+  for (int c = 0; c < 300; ++c) {
+    float strain[6], ratio[6];
+    int lk[6];
+    bool has[6], extT[3];
+    for (int i = 0; i < 6; ++i) {
+      has[i] = rng() % 5 != 0;
+      lk[i] = has[i] ? i : -1;
+      strain[i] = (float)U(-2e-3, 2e-3);
+      ratio[i] = (float)std::exp(U(std::log(0.5), std::log(2.0)));
+    }
+    vxg_external ext;
+    std::memset(&ext, 0, sizeof(ext));
+    int vext[1] = {-1};
+    if (rng() % 2) {
+      vext[0] = 0;
+      ext.dof = (int)(rng() % 8);
+      ext.force[rng() % 3] = 0.01f;
+    }
+    for (int i = 0; i < 3; ++i) extT[i] = vext[0] >= 0 && ((ext.dof & (1 << i)) != 0 || ext.force[i] != 0);
+    vxg_voxel_material vm;
+    std::memset(&vm, 0, sizeof(vm));
+    vm.nu = 0.3f;
+    vm.powf_slot = -1;
+    int vmat[1] = {0};
+    vx64::Ctl ctl;
+    std::memset(&ctl, 0, sizeof(ctl));
+    vx64::View S;
+    std::memset(&S, 0, sizeof(S));
+    S.nv = 1; S.nl = 6; S.vmat = vmat; S.vext = vext; S.ext = &ext; S.vm = &vm; S.ctl = &ctl;
+    S.strain = strain; S.strainRatio = ratio;
+    auto P = [&](int k) { float out[3]; vx64::poisson_strain_links(S, 0, lk, out); return (double)out[k]; };
+    for (int k = 0; k < 3; ++k) {
+      double gP[3] = {0, 0, 0};
+      gP[k] = 1.0;
+      float e[6];
+      for (int i = 0; i < 6; ++i) e[i] = (i & 1) ? 2.0f * strain[i] * ratio[i] / (1.0f + ratio[i]) : 2.0f * strain[i] / (1.0f + ratio[i]);
+      double ge[6] = {0, 0, 0, 0, 0, 0};
+      poisson_adjoint(e, has, extT, vm.nu, gP, ge);
+      std::vector<double> fd, ad;
+      for (int i = 0; i < 6; ++i) {
+        if (!has[i]) continue;
+        const double r = ratio[i];
+        const double de = (i & 1) ? 2.0 * r / (1.0 + r) : 2.0 / (1.0 + r);  // d(end strain)/d(strain)
+        float s0 = strain[i];  // a wide step: the result is powf(1 + sum, -nu) - 1 rounded to float
+        strain[i] = s0 + 4e-4f; double hp = (double)strain[i] - s0; double jp = P(k);
+        strain[i] = s0 - 4e-4f; double hm = s0 - (double)strain[i]; double jm = P(k);
+        strain[i] = s0;
+        fd.push_back((jp - jm) / (hp + hm));
+        ad.push_back(ge[i] * de);
+      }
+      cp.tag = k;
+      cp.row(fd, ad);
+    }
+    pcases++;
+  }
+  printf("%s %.3e %d %d\n", cp.name, cp.err, cp.n, pcases);
   return (bad_forward || bad_vforward) ? 1 : 0;
 }

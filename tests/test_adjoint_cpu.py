@@ -3,7 +3,10 @@ with g++: its forward recomputation matches vx64::link_update / vx64::voxel_upda
 random inputs, and its derivatives match central differences of that forward output by output
 (worst relative error, floored at 1e-4 of each output's largest gradient component, below 2e-3).
 Large-angle links (both frame formulas of orientLink, strains of 0.1-0.6): the difference nearest
-the adjoint among six steps, floored at 1e-3 of each output's largest component, below 5e-3."""
+the adjoint among six steps, floored at 1e-3 of each output's largest component, below 5e-3.
+Links with Poisson's ratio 0.3 also take their ends' Poisson strains as inputs and give the axial
+strain as an output; a voxel's Poisson strains (CVX_Voxel::strain(true)) are checked against
+differences of vx64::poisson_strain_links with respect to its links' strains, below 2e-3."""
 from __future__ import annotations
 
 import os
@@ -29,4 +32,5 @@ def test_adjoint_against_finite_differences_on_cpu(tmp_path):
     assert res["voxel_forward_mismatch"][0] == 0
     assert res["link"][1] > 10000 and res["link"][0] < 2e-3
     assert res["link_large"][2] >= 100 and res["link_large"][0] < 5e-3
+    assert res["poisson"][1] > 1000 and res["poisson"][0] < 2e-3
     assert res["voxel"][1] > 10000 and res["voxel"][0] < 2e-3

@@ -140,6 +140,33 @@ def test_adjoint_with_partial_fixes(product_lib):
         assert two <= 1e-4 and inf <= 1e-4
 
 
+def test_adjoint_with_poisson_ratio(product_lib):
+    """Poisson's ratio 0.3 for every voxel (CVX_Link::updateTransverseInfo and CVX_Voxel::strain
+    (true)): each link's stress takes the transverse strain sum and its axial force the transverse
+    area of its two voxels, whose Poisson strains the pre-pass recomputes from the previous step's
+    link strains and the links' strain ratios (E of one end over E of the other); the adjoint
+    carries both back.  The bending cantilevers (no floor, so no contact decisions), 200 steps.
+    The reference rounds powf(1 + sum, -nu) - 1 to float, which quantises the Poisson strains and
+    makes the differences ragged: where the two differences (4e-3 relative and 0.04 rad, and a
+    quarter of each) agree within 1 %, the adjoint lies within 1e-3 of the interval they span."""
+    sc = _beams()
+    for m in sc.materials:
+        m.nu = 0.3
+    off = G.body_offsets(sc)
+    rng = np.random.default_rng(3)
+    kinds = ["E", "rho", "phase"]
+    free = lambda b: [v for v in range(off[b], off[b + 1]) if sc.xyz[v, 0] > 0]
+    pick = [(b, int(rng.choice(free(b))), kinds[b % 3]) for b in range(len(off) - 1)]
+    rows, _, _, _ = G.check(product_lib, sc, 200, 50, pick, 4e-3, 0.04, AMP, FREQ, frozen=True)
+    for (b, v, kind), r in zip(pick, rows):
+        print("body %3d voxel %5d d/d%-5s adjoint % .6e D(h) % .6e D(h/4) % .6e distance %.2e"
+              % (b, v, kind, r["adjoint"], r["fd_h"], r["fd_h4"], r["distance"]))
+    smooth = [abs(r["fd_h"] - r["fd_h4"]) <= 1e-2 * max(abs(r["fd_h"]), abs(r["fd_h4"])) for r in rows]
+    print(f"{sum(smooth)} of {len(rows)} parameters with agreeing differences")
+    assert sum(smooth) >= 5 and {k for (b, v, k), s in zip(pick, smooth) if s} == set(kinds)
+    assert max(r["distance"] for r, s in zip(rows, smooth) if s) <= 1e-3
+
+
 def _beams(n=8, length=12, E_range=(1e4, 3e4), seed=7, tip=-0.05, fail_strain=None):
     """n soft cantilevers of length x 2 x 2 cells (one material per voxel, E log-uniform in E_range,
     density 1000, CTE 0.01), fixed at x = 0, each of the four tip voxels pulled down by `tip` N,

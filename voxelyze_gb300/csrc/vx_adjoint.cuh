@@ -183,7 +183,59 @@ struct LinkIn {
   float dmN, dmP;        // damping multipliers 2 sqrt(m) zeta / previous dt of the two voxels
   float maxStrain;       // the largest axial strain so far (CVX_Link::maxStrain) at the step's start
   float epsilonFail;     // the material's failure strain, -1: none
+  // Poisson's ratio of the link material and its eHat (nu = 0: the stored transverse area tArea is
+  // used), and each end voxel's transverse data: its material's nominal size, whether that
+  // material has nu != 0, and its Poisson strains this step (CVX_Voxel::poissonsStrain)
+  float nu, eHat;
+  float sizeN, sizeP;
+  bool nuN, nuP;
+  d3 psn, psp;
 };
+// CVX_Voxel::transverseArea / transverseStrainSum across the link's axis (vx64::transverse_area's
+// and vx64::transverse_strain_sum's arithmetic) and their adjoints with respect to the Poisson strains
+VX_HD float transverse_area_of(float size, bool hasNu, const d3& ps, int axis) {
+  if (!hasNu) return size * size;
+  switch (axis) {
+    case 0: return (float)(size * size * (1 + ps.y) * (1 + ps.z));
+    case 1: return (float)(size * size * (1 + ps.x) * (1 + ps.z));
+    default: return (float)(size * size * (1 + ps.x) * (1 + ps.y));
+  }
+}
+VX_HD float transverse_strain_sum_of(bool hasNu, const d3& ps, int axis) {
+  if (!hasNu) return 0;
+  const float px = (float)ps.x, py = (float)ps.y, pz = (float)ps.z;
+  switch (axis) {
+    case 0: return py + pz;
+    case 1: return px + pz;
+    default: return px + py;
+  }
+}
+VX_HD void transverse_adj(float size, bool hasNu, const d3& ps, int axis, double gTA, double gTS, d3& gps) {
+  if (!hasNu) return;
+  const double s2 = (double)(size * size);
+  switch (axis) {
+    case 0: gps.y += gTA * s2 * (1 + ps.z) + gTS; gps.z += gTA * s2 * (1 + ps.y) + gTS; break;
+    case 1: gps.x += gTA * s2 * (1 + ps.z) + gTS; gps.z += gTA * s2 * (1 + ps.x) + gTS; break;
+    default: gps.x += gTA * s2 * (1 + ps.y) + gTS; gps.y += gTA * s2 * (1 + ps.x) + gTS;
+  }
+}
+// the link's transverse area and strain sum this step (CVX_Link::updateTransverseInfo,
+// VX_Link.cpp:142-147, for nu != 0; the stored area otherwise)
+VX_HD void link_transverse(const LinkIn& in, float* tArea, float* tSS) {
+  *tArea = in.tArea;
+  *tSS = 0.0f;
+  if (in.nu != 0.0f) {
+    *tArea = 0.5f * (transverse_area_of(in.sizeN, in.nuN, in.psn, in.axis) +
+                     transverse_area_of(in.sizeP, in.nuP, in.psp, in.axis));
+    *tSS = 0.5f * (transverse_strain_sum_of(in.nuN, in.psn, in.axis) + transverse_strain_sum_of(in.nuP, in.psp, in.axis));
+  }
+}
+// CVX_Material::stress for a linear material (vx64::mat_stress)
+VX_HD float link_stress(const LinkIn& in, float strain, float tss) {
+  if (in.epsilonFail != -1.0f && strain > in.epsilonFail) return 0.0f;
+  if (in.nu == 0.0f) return in.E * strain;
+  return in.eHat * ((1 - in.nu) * strain + in.nu * tss);
+}
 struct LinkOut {
   d3 fN, fP, mN, mP;     // in the voxels' frames, original axes (what the voxel pass gathers)
   d3 pos2, a1v, a2v;
@@ -305,11 +357,13 @@ VX_HD LinkOut link_forward(const LinkIn& in) {
   d3 dPos2 = D3(0.5 * (pos2.x - in.oldPos2.x), 0.5 * (pos2.y - in.oldPos2.y), 0.5 * (pos2.z - in.oldPos2.z));
   d3 dA1 = D3(0.5 * (a1v.x - in.oldA1.x), 0.5 * (a1v.y - in.oldA1.y), 0.5 * (a1v.z - in.oldA1.z));
   d3 dA2 = D3(0.5 * (a2v.x - in.oldA2.x), 0.5 * (a2v.y - in.oldA2.y), 0.5 * (a2v.z - in.oldA2.z));
+  float tArea, tSS;
+  link_transverse(in, &tArea, &tSS);
   float axial = (float)(pos2.x / in.rest);
-  float stress = in.E * axial;
+  float stress = link_stress(in, axial, tSS);
   o.failed = link_failed(in, axial, &o.maxStrain);
   float b1 = in.b1, b2 = in.b2, b3 = in.b3, a2 = in.a2;
-  d3 fN = D3((double)(stress * in.tArea), b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
+  d3 fN = D3((double)(stress * tArea), b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
   d3 fP = D3(-fN.x, -fN.y, -fN.z);
   d3 mN = D3(a2 * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (2 * a1v.y + a2v.y), b2 * pos2.y - b3 * (2 * a1v.z + a2v.z));
   d3 mP = D3(a2 * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z));
@@ -357,13 +411,15 @@ struct LinkGrad {
   q4 gqn, gqp;
   d3 gOldPos2, gOldA1, gOldA2;
   double gRest, gE, gDmN, gDmP;  // gE: with respect to the link material's E (all constants scale with it)
+  d3 gpsn, gpsp;                 // with respect to the end voxels' Poisson strains this step
 };
 
 // Adjoint of link_forward, in both branches of orientLink, along the branch the step takes.
 // gfN..gmP: adjoints of the four force/moment outputs; gPos2, gA1v, gA2v: of the new link pose
-// (read by the next step's damping terms).
+// (read by the next step's damping terms); gAxial: of the new axial strain (read by the next
+// step's Poisson strains).
 VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, const d3& gmN_o, const d3& gmP_o,
-                        const d3& gPos2_in, const d3& gA1v_in, const d3& gA2v_in, LinkGrad& g) {
+                        const d3& gPos2_in, const d3& gA1v_in, const d3& gA2v_in, double gAxial_in, LinkGrad& g) {
   // ---- forward recomputation ----
   d3 D = vx64::to_axis_x(in.axis, D3(in.pp.x - in.pn.x, in.pp.y - in.pn.y, in.pp.z - in.pn.z));
   q4 A1 = vx64::to_axis_x(in.axis, in.qn);
@@ -398,10 +454,12 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
   d3 dP = D3(0.5 * (p.x - in.oldPos2.x), 0.5 * (p.y - in.oldPos2.y), 0.5 * (p.z - in.oldPos2.z));
   d3 dA1 = D3(0.5 * (a1.x - in.oldA1.x), 0.5 * (a1.y - in.oldA1.y), 0.5 * (a1.z - in.oldA1.z));
   d3 dA2 = D3(0.5 * (a2v.x - in.oldA2.x), 0.5 * (a2v.y - in.oldA2.y), 0.5 * (a2v.z - in.oldA2.z));
+  float tArea, tSS;
+  link_transverse(in, &tArea, &tSS);
   double axial = (double)(float)(p.x / in.rest);
-  float stress = in.E * (float)axial;
+  float stress = link_stress(in, (float)axial, tSS);
   const double b1 = in.b1, b2 = in.b2, b3 = in.b3, a2c = in.a2;
-  d3 fN0 = D3((double)(stress * in.tArea), b1 * p.y - b2 * (a1.z + a2v.z), b1 * p.z + b2 * (a1.y + a2v.y));
+  d3 fN0 = D3((double)(stress * tArea), b1 * p.y - b2 * (a1.z + a2v.z), b1 * p.z + b2 * (a1.y + a2v.y));
   d3 mN0 = D3(a2c * (a2v.x - a1.x), -b2 * p.z - b3 * (2 * a1.y + a2v.y), b2 * p.y - b3 * (2 * a1.z + a2v.z));
   d3 mP0 = D3(a2c * (a1.x - a2v.x), -b2 * p.z - b3 * (a1.y + 2 * a2v.y), b2 * p.y - b3 * (a1.z + 2 * a2v.z));
   d3 fN = fN0, mN = mN0;
@@ -472,7 +530,8 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
   // fP0 = -fN0
   gfN0.x -= gfP0.x; gfN0.y -= gfP0.y; gfN0.z -= gfP0.z;
   // fN0
-  double gstress = (double)in.tArea * gfN0.x;
+  double gstress = (double)tArea * gfN0.x;
+  const double gtArea = (double)stress * gfN0.x;
   gp.y += b1 * gfN0.y; ga1.z -= b2 * gfN0.y; ga2.z -= b2 * gfN0.y;
   gb1 += p.y * gfN0.y; gb2 -= (a1.z + a2v.z) * gfN0.y;
   gp.z += b1 * gfN0.z; ga1.y += b2 * gfN0.z; ga2.y += b2 * gfN0.z;
@@ -489,10 +548,25 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
   gb2 -= p.z * gmP0.y; gb3 -= (a1.y + 2 * a2v.y) * gmP0.y;
   gp.y += b2 * gmP0.z; ga1.z -= b3 * gmP0.z; ga2.z -= 2 * b3 * gmP0.z;
   gb2 += p.y * gmP0.z; gb3 -= (a1.z + 2 * a2v.z) * gmP0.z;
-  // stress = E axial ; axial = p.x / rest
+  // stress = E axial (nu = 0) or eHat ((1 - nu) axial + nu tSS), zero past the failure strain;
+  // axial = p.x / rest, whose adjoint also comes from the next step's Poisson strains (gAxial_in)
   double E = in.E;
-  double gaxial = E * gstress;
-  double gE = axial * gstress;
+  double gaxial = gAxial_in, gtSS = 0, gE = 0;
+  if (!(in.epsilonFail != -1.0f && (float)axial > in.epsilonFail)) {
+    if (in.nu == 0.0f) {
+      gaxial += E * gstress;
+    } else {
+      gaxial += (double)in.eHat * (1 - in.nu) * gstress;
+      gtSS = (double)in.eHat * in.nu * gstress;
+    }
+    gE = (E != 0 ? (double)stress / E : 0.0) * gstress;  // eHat is proportional to E
+  }
+  g.gpsn = D3(0, 0, 0);
+  g.gpsp = D3(0, 0, 0);
+  if (in.nu != 0.0f) {  // tArea, tSS: the means of the two ends' transverse terms
+    transverse_adj(in.sizeN, in.nuN, in.psn, in.axis, 0.5 * gtArea, 0.5 * gtSS, g.gpsn);
+    transverse_adj(in.sizeP, in.nuP, in.psp, in.axis, 0.5 * gtArea, 0.5 * gtSS, g.gpsp);
+  }
   gp.x += gaxial / in.rest;
   double grest = -p.x / (in.rest * in.rest) * gaxial;
   // dP, dA1, dA2
@@ -536,6 +610,44 @@ VX_HD bool link_adjoint(const LinkIn& in, const d3& gfN_o, const d3& gfP_o, cons
   g.gE = gE + (gb1 * b1 + gb2 * b2 + gb3 * b3 + ga2c * a2c) / Ed +
          0.5 * (gsqA1 * sqA1 + gsqA2 * sqA2 + gsqB1 * sqB1 + gsqB2 * sqB2 + gsqB3 * sqB3) / Ed;
   return true;
+}
+
+// CVX_Voxel::strain(true) (vx64::poisson_strain_links, VX_Voxel.cpp:300-334) differentiated with
+// respect to the axial strains its links' ends see: e[i] for slot i where has[i]; extT[i]: an
+// external fixes or loads axis i (which makes an axis with one link count as in tension); gP: the
+// adjoint of the three Poisson strains; adds into ge.
+VX_HD void poisson_adjoint(const float e[6], const bool has[6], const bool extT[3], float nu, const double gP[3],
+                           double ge[6]) {
+  float s[3] = {0, 0, 0};
+  int nb[3] = {0, 0, 0};
+  for (int i = 0; i < 6; ++i)
+    if (has[i]) {
+      s[i / 2] += e[i];
+      nb[i / 2]++;
+    }
+  bool tension[3];
+  for (int i = 0; i < 3; ++i) {
+    if (nb[i] == 2) s[i] *= 0.5f;
+    tension[i] = nb[i] == 2 || (nb[i] == 1 && extT[i]);
+  }
+  double gs[3] = {0, 0, 0};
+  for (int i = 0; i < 3; ++i)
+    if (tension[i]) gs[i] += gP[i];
+  if (!(tension[0] && tension[1] && tension[2])) {  // the other axes: powf(1 + sum, -nu) - 1
+    float add = 0;
+    for (int i = 0; i < 3; ++i)
+      if (tension[i]) add += s[i];
+    double gval = 0;
+    for (int i = 0; i < 3; ++i)
+      if (!tension[i]) gval += gP[i];
+    const double gadd = gval * (-(double)nu * pow(1.0 + (double)add, -(double)nu - 1.0));
+    for (int i = 0; i < 3; ++i)
+      if (tension[i]) gs[i] += gadd;
+  }
+  for (int i = 0; i < 3; ++i)
+    if (nb[i] == 2) gs[i] *= 0.5;
+  for (int i = 0; i < 6; ++i)
+    if (has[i]) ge[i] += gs[i / 2];
 }
 
 // ---- voxel -----------------------------------------------------------------------------------

@@ -30,6 +30,11 @@ struct AdjBuf {
   double* tl;           // K x 9 nl: pos2 3, angle1v 3, angle2v 3
   uint32_t* tlf;        // K x nl link flags
   float* tms;           // K x nl largest axial strain so far (failure)
+  float* tstrain;       // K x nl axial strain at the step's start (the previous step's, nu != 0)
+  float* tps;           // K x 3 nv Poisson strains the step's links used (nu != 0)
+  double* lps;          // 6 nl: adjoints of the negative and positive voxels' Poisson strains
+  double* gS;           // 6 nv: adjoint of the axial strain each voxel's slot-i link shows it, from
+                        // the Poisson strains of the step after (read by the link adjoint)
   float* ttime;         // K step start times
   float* ttemp;         // K x nv temperatures each step used (after its actuation)
   double* tforce;       // K x 12 nl link forces and moments of each step (null: recomputed)
@@ -57,7 +62,10 @@ __device__ __forceinline__ double act_dtemp_dphase(const ActParams& A, int v, fl
 __global__ void k_tape_step(View S, AdjBuf T, int slot) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nv = S.nv, nl = S.nl;
-  if (i < nv) T.ttemp[(size_t)slot * nv + i] = S.temp[i];
+  if (i < nv) {
+    T.ttemp[(size_t)slot * nv + i] = S.temp[i];
+    for (int c = 0; c < 3; ++c) T.tps[((size_t)slot * 3 + c) * nv + i] = S.pStrain[(size_t)c * nv + i];
+  }
   if (T.tforce && i < nl) {
     double* tf = T.tforce + (size_t)slot * 12 * nl;
     for (int c = 0; c < 3; ++c) {
@@ -92,6 +100,7 @@ __global__ void k_tape_save(View S, AdjBuf T, int slot) {
     }
     T.tlf[(size_t)slot * nl + i] = S.lflags[i];
     T.tms[(size_t)slot * nl + i] = S.maxStrain[i];
+    T.tstrain[(size_t)slot * nl + i] = S.strain[i];
   }
   if (i == 0) T.ttime[slot] = S.ctl->time;
 }
@@ -128,6 +137,15 @@ __device__ vxa::LinkIn tape_link_in(const View& S, const AdjBuf& T, const ActPar
   in.tArea = S.tArea[l];
   in.maxStrain = T.tms[(size_t)slot * nl + l];
   in.epsilonFail = m.epsilonFail;
+  in.nu = m.nu;
+  in.eHat = m.eHat;
+  in.sizeN = (float)mn.nomSize;
+  in.sizeP = (float)mp.nomSize;
+  in.nuN = mn.nu != 0.0f;
+  in.nuP = mp.nu != 0.0f;
+  const float* ps = T.tps + (size_t)slot * 3 * nv;
+  in.psn = vx64::D3(ps[vn], ps[nv + vn], ps[2 * nv + vn]);
+  in.psp = vx64::D3(ps[vp], ps[nv + vp], ps[2 * nv + vp]);
   // CVX_Voxel::dampingMultiplier with the previous dt the step saw (VX_Voxel.h:130)
   in.dmN = 2 * mn.sqrtMass * mn.zetaInternal / T.tpd[(size_t)slot * nv + vn];
   in.dmP = 2 * mp.sqrtMass * mp.zetaInternal / T.tpd[(size_t)slot * nv + vp];
@@ -244,12 +262,21 @@ __global__ void k_adj_link(View S, AdjBuf T, ActParams A, int slot) {
   vx64::d3 gPos2 = vx64::D3(T.mu[l], T.mu[nl + l], T.mu[2 * nl + l]);
   vx64::d3 gA1v = vx64::D3(T.mu[3 * nl + l], T.mu[4 * nl + l], T.mu[5 * nl + l]);
   vx64::d3 gA2v = vx64::D3(T.mu[6 * nl + l], T.mu[7 * nl + l], T.mu[8 * nl + l]);
+  // the axial strain's adjoint from the next step's Poisson strains: this link is the negative
+  // voxel's slot 2 axis and the positive voxel's slot 2 axis + 1 (vx64::link_axial_strain's ends)
+  double gAxial = 0;
+  if (in.nu != 0.0f) {
+    const double r = S.strainRatio[l];
+    gAxial = T.gS[(size_t)(2 * in.axis) * nv + vn] * (2.0 / (1.0 + r)) +
+             T.gS[(size_t)(2 * in.axis + 1) * nv + vp] * (2.0 * r / (1.0 + r));
+  }
   vxa::LinkGrad g;
-  if (!vxa::link_adjoint(in, gfN, gfP, gmN, gmP, gPos2, gA1v, gA2v, g)) {
+  if (!vxa::link_adjoint(in, gfN, gfP, gmN, gmP, gPos2, gA1v, gA2v, gAxial, g)) {
     atomicOr(T.err, 1);
     for (int c = 0; c < 9; ++c) T.mu[(size_t)c * nl + l] = 0.0;
     for (int c = 0; c < 14; ++c) T.lcon[(size_t)c * nl + l] = 0.0;
     for (int c = 0; c < 4; ++c) T.lpar[(size_t)c * nl + l] = 0.0;
+    for (int c = 0; c < 6; ++c) T.lps[(size_t)c * nl + l] = 0.0;
     return;
   }
   const double mu[9] = {g.gOldPos2.x, g.gOldPos2.y, g.gOldPos2.z, g.gOldA1.x, g.gOldA1.y, g.gOldA1.z,
@@ -260,6 +287,8 @@ __global__ void k_adj_link(View S, AdjBuf T, ActParams A, int slot) {
   for (int c = 0; c < 14; ++c) T.lcon[(size_t)c * nl + l] = con[c];
   const double par[4] = {g.gRest, g.gE, g.gDmN, g.gDmP};
   for (int c = 0; c < 4; ++c) T.lpar[(size_t)c * nl + l] = par[c];
+  const double lps[6] = {g.gpsn.x, g.gpsn.y, g.gpsn.z, g.gpsp.x, g.gpsp.y, g.gpsp.z};
+  for (int c = 0; c < 6; ++c) T.lps[(size_t)c * nl + l] = lps[c];
 }
 
 __global__ void k_adj_gather(View S, AdjBuf T, ActParams A, int slot) {
@@ -268,7 +297,7 @@ __global__ void k_adj_gather(View S, AdjBuf T, ActParams A, int slot) {
   if (v >= nv) return;
   const vxg_voxel_material& m = S.vm[S.vmat[v]];
   double lam[7] = {0, 0, 0, 0, 0, 0, 0};  // pos 3, orient 4
-  double gE = 0, gSqrtMass = 0, gTemp = T.gTempV[v];
+  double gE = 0, gSqrtMass = 0, gTemp = T.gTempV[v], gP[3] = {0, 0, 0};
   float pdt = T.tpd[(size_t)slot * nv + v];
   for (int i = 0; i < 6; ++i) {
     int l = S.vlinks[i * nv + v];
@@ -276,6 +305,7 @@ __global__ void k_adj_gather(View S, AdjBuf T, ActParams A, int slot) {
     bool neg = (i & 1) == 0;  // even slots (X+, Y+, Z+): this voxel is the link's negative end
     int o = neg ? 0 : 7;
     for (int c = 0; c < 7; ++c) lam[c] += T.lcon[(size_t)(o + c) * nl + l];
+    for (int c = 0; c < 3; ++c) gP[c] += T.lps[(size_t)((neg ? 0 : 3) + c) * nl + l];
     double gDm = T.lpar[(size_t)(neg ? 2 : 3) * nl + l];
     if (gDm != 0.0) gSqrtMass += gDm * (2.0 * (double)m.zetaInternal / (double)pdt);
     int other = neg ? S.lvox[nl + l] : S.lvox[l];
@@ -294,6 +324,50 @@ __global__ void k_adj_gather(View S, AdjBuf T, ActParams A, int slot) {
     T.accRho[v] += gSqrtMass * 0.5 / (double)m.sqrtMass * volume;
   }
   if (A.mode == 2) T.accPhase[v] += gTemp * act_dtemp_dphase(A, v, T.ttime[slot]);
+  // the Poisson strains this step's links used, where the pre-pass recomputed them (the cache was
+  // invalid at the step's start), from the previous step's axial strains: their adjoints, per slot,
+  // for that step's link adjoint (elsewhere the cache is a constant: nothing flows back)
+  double ge[6] = {0, 0, 0, 0, 0, 0};
+  if (m.nu != 0.0f && (T.tvf[(size_t)slot * nv + v] & VXG_VF_PSTRAIN_INVALID) && (gP[0] != 0 || gP[1] != 0 || gP[2] != 0)) {
+    float e[6];
+    bool has[6], extT[3] = {false, false, false};
+    for (int i = 0; i < 6; ++i) {
+      const int l = S.vlinks[i * nv + v];
+      has[i] = l >= 0;
+      e[i] = 0.0f;
+      if (has[i]) {  // vx64::link_axial_strain at this voxel's end
+        const float s = T.tstrain[(size_t)slot * nl + l], r = S.strainRatio[l];
+        e[i] = (i & 1) ? 2.0f * s * r / (1.0f + r) : 2.0f * s / (1.0f + r);
+      }
+    }
+    const int ei = S.vext[v];
+    if (ei >= 0)
+      for (int i = 0; i < 3; ++i) extT[i] = (S.ext[ei].dof & (1 << i)) != 0 || S.ext[ei].force[i] != 0;
+    vxa::poisson_adjoint(e, has, extT, m.nu, gP, ge);
+  }
+  for (int c = 0; c < 6; ++c) T.gS[(size_t)c * nv + v] = ge[c];
+}
+
+// After k_adj_gather, where some Poisson's ratio is not 0: the end strains a voxel's Poisson strains
+// read are 2 s / (1 + r) and 2 s r / (1 + r) with the link's strain ratio r = E(positive voxel) /
+// E(negative voxel) (CVX_Link::axialStrain): their adjoints (gS, this step) reach both voxels'
+// Young's moduli through r.  One thread per voxel over its links, so no atomics.
+__global__ void k_adj_ratio(View S, AdjBuf T, int slot) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = S.nv, nl = S.nl;
+  if (v >= nv) return;
+  const double Ev = S.vm[S.vmat[v]].E;
+  double g = 0;
+  for (int i = 0; i < 6; ++i) {
+    const int l = S.vlinks[i * nv + v];
+    if (l < 0) continue;
+    const int a = i / 2, vn = S.lvox[l], vp = S.lvox[nl + l];
+    const double s = T.tstrain[(size_t)slot * nl + l], r = S.strainRatio[l];
+    const double d = 2.0 * s / ((1.0 + r) * (1.0 + r));  // -d(2 s / (1 + r))/dr = d(2 s r / (1 + r))/dr
+    const double gr = -T.gS[(size_t)(2 * a) * nv + vn] * d + T.gS[(size_t)(2 * a + 1) * nv + vp] * d;
+    g += (v == vp ? 1.0 : -1.0) * gr * r / Ev;
+  }
+  T.accE[v] += g;
 }
 
 // Objective: sum over bodies of the mass-weighted centre-of-mass x.  One block per body (contiguous

@@ -1598,10 +1598,11 @@ int vxg_set_tables(vxg_engine* e, const vxg_voxel_material* vm, int n_vm, const 
     if (vm[k].nu != 0.0f) e->tab_poisson = true;
   e->adj_scope = nullptr;
   for (int k = 0; k < n_lm && !e->adj_scope; ++k)
-    if (!lm[k].linear || lm[k].nu != 0.0f)
-      e->adj_scope = "a link material is not linear or has Poisson's ratio != 0";
-  for (int k = 0; k < n_vm && !e->adj_scope; ++k)
-    if (vm[k].nu != 0.0f) e->adj_scope = "a voxel material has Poisson's ratio != 0";
+    if (!lm[k].linear) e->adj_scope = "a link material is not linear";
+  // one Poisson's ratio for every voxel material: a link's ratio then depends on no Young's modulus
+  // (CVX_MaterialLink combines the two eHat)
+  for (int k = 1; k < n_vm && !e->adj_scope; ++k)
+    if (vm[k].nu != vm[0].nu) e->adj_scope = "voxel materials with different Poisson's ratios";
   VXG_CK(cudaStreamSynchronize(e->stream));
   rebuild_view(e);
   return VXG_OK;
@@ -2319,7 +2320,6 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
     return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: branch decisions are being recorded or replayed (mode 0 first)");
   if (e->adj_scope) return fail(e, VXG_E_STATE, e->adj_scope);
   if (e->g.collisions) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: collisions are outside the differentiated scope");
-  if (e->g.any_poisson) return fail(e, VXG_E_STATE, "vxg_adjoint_com_x: Poisson's ratio must be 0");
   if (e->act_mode == 2 && e->n_phase < e->nv) return fail(e, VXG_E_STATE, "actuation phases cover fewer voxels than the scene");
   for (int b = 0; b < n_bodies; ++b)
     if (body_offsets[b] < 0 || body_offsets[b + 1] < body_offsets[b] || body_offsets[b + 1] > e->nv)
@@ -2335,6 +2335,8 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   size_t o_tv = carve(sizeof(double) * 13 * (size_t)nv * K), o_tvf = carve(sizeof(uint32_t) * (size_t)nv * K),
          o_tpd = carve(sizeof(float) * (size_t)nv * K), o_tl = carve(sizeof(double) * 9 * (size_t)nl * K),
          o_tlf = carve(sizeof(uint32_t) * (size_t)nl * K), o_tms = carve(sizeof(float) * (size_t)nl * K),
+         o_tstr = carve(sizeof(float) * (size_t)nl * K), o_tps = carve(sizeof(float) * 3 * (size_t)nv * K),
+         o_lps = carve(sizeof(double) * 6 * (size_t)nl), o_gs = carve(sizeof(double) * 6 * (size_t)nv),
          o_tt = carve(sizeof(float) * K),
          o_ttemp = carve(sizeof(float) * (size_t)nv * K),
          o_lam = carve(sizeof(double) * 13 * (size_t)nv), o_gfm = carve(sizeof(double) * 6 * (size_t)nv),
@@ -2361,6 +2363,10 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   T.tv = (double*)(buf + o_tv); T.tvf = (uint32_t*)(buf + o_tvf); T.tpd = (float*)(buf + o_tpd);
   T.tl = (double*)(buf + o_tl); T.tlf = (uint32_t*)(buf + o_tlf); T.ttime = (float*)(buf + o_tt);
   T.tms = (float*)(buf + o_tms);
+  T.tstrain = (float*)(buf + o_tstr);
+  T.tps = (float*)(buf + o_tps);
+  T.lps = (double*)(buf + o_lps);
+  T.gS = (double*)(buf + o_gs);
   T.ttemp = (float*)(buf + o_ttemp);
   T.tforce = o_tf ? (double*)(buf + o_tf) : nullptr;
   T.lam = (double*)(buf + o_lam); T.gFM = (double*)(buf + o_gfm); T.mu = (double*)(buf + o_mu);
@@ -2393,6 +2399,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
   if ((rc = save(nck))) return rc;
   VXG_CK(cudaMemsetAsync(T.lam, 0, sizeof(double) * 13 * (size_t)nv, e->stream));
   VXG_CK(cudaMemsetAsync(T.mu, 0, sizeof(double) * 9 * (size_t)nl, e->stream));
+  VXG_CK(cudaMemsetAsync(T.gS, 0, sizeof(double) * 6 * (size_t)nv, e->stream));
   VXG_CK(cudaMemsetAsync(T.accE, 0, sizeof(double) * 3 * (size_t)nv, e->stream));
   VXG_CK(cudaMemsetAsync(T.err, 0, sizeof(int), e->stream));
   VXG_CK(cudaMemcpyAsync(d_off, body_offsets, sizeof(int) * ((size_t)n_bodies + 1), cudaMemcpyHostToDevice, e->stream));
@@ -2415,6 +2422,7 @@ int vxg_adjoint_com_x(vxg_engine* e, int nsteps, float dt, int checkpoint_every,
       k_adj_voxel<<<gvx, kBlock, 0, e->stream>>>(e->S, Ts, A, s, dt);
       if (nl) k_adj_link<<<glk, kBlock, 0, e->stream>>>(e->S, T, A, s);
       k_adj_gather<<<gvx, kBlock, 0, e->stream>>>(e->S, T, A, s);
+      if (e->g.any_poisson) k_adj_ratio<<<gvx, kBlock, 0, e->stream>>>(e->S, T, s);
     }
     VXG_CK(cudaGetLastError());
   }
