@@ -25,3 +25,30 @@ def test_cantilever_size():
     sc = S.cantilever(40, 8, 8)
     assert sc.n_voxels == 2_560
     assert _links(sc.xyz) == 6_976
+
+
+def _pieces(xyz):
+    """Starts of the runs of the voxel order that no link crosses: the cut rule of the engine's
+    body batches (a difference array over each link's end indices)."""
+    n = len(xyz)
+    index = {tuple(p): i for i, p in enumerate(xyz)}
+    cover = np.zeros(n + 1, np.int64)
+    for i, p in enumerate(xyz):
+        for d in ((1, 0, 0), (0, 1, 0), (0, 0, 1)):
+            j = index.get((p[0] + d[0], p[1] + d[1], p[2] + d[2]))
+            if j is not None:
+                a, b = min(i, j), max(i, j)
+                cover[a] += 1
+                cover[b] -= 1
+    run = np.cumsum(cover[:n])
+    return np.concatenate([[0], np.flatnonzero(run[:-1] == 0) + 1])
+
+
+def test_population_bodies_are_pieces():
+    """Body batches need each body to be a run of the voxel order that no link crosses: the
+    population generator adds body after body with gaps between them, and each body is one
+    connected component, so its pieces are exactly its bodies."""
+    sc = S.population(64)
+    starts = _pieces(sc.xyz)
+    offsets = np.concatenate([[0], np.cumsum(np.bincount(sc.body))])[:-1]
+    assert np.array_equal(starts, offsets)
