@@ -2,7 +2,6 @@
 declare (include/vxg.h, include/vx_capi.h).  No compute call is made here."""
 from __future__ import annotations
 
-import ctypes
 import os
 import re
 

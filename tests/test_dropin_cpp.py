@@ -2,7 +2,6 @@
 product library (compile check on CPU; run and compare with the oracle on the GPU)."""
 from __future__ import annotations
 
-import ctypes as C
 import os
 import subprocess
 

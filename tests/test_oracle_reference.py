@@ -9,7 +9,6 @@
 """
 from __future__ import annotations
 
-import ctypes as C
 import json
 import os
 import platform
