@@ -528,9 +528,9 @@ bool CVoxelyze::flush() {
   }
   if (I.topo_dirty && I.act_mode) I.act_dirty = true;
   const int nv = (int)voxelsList.size(), nl = (int)linksList.size();
-  std::unordered_map<const CVX_MaterialVoxel*, int> vmi;
-  for (size_t k = 0; k < voxelMats.size(); ++k) vmi[voxelMats[k]] = (int)k;
   if (I.topo_dirty) {
+    std::unordered_map<const CVX_MaterialVoxel*, int> vmi;
+    for (size_t k = 0; k < voxelMats.size(); ++k) vmi[voxelMats[k]] = (int)k;
     if (vxg_resize(I.eng, nv, nl)) { I.err = vxg_last_error(I.eng); return false; }
     std::vector<int> a((size_t)nv), idx3((size_t)3 * nv), lk((size_t)6 * nv);
     for (int i = 0; i < nv; ++i) {
