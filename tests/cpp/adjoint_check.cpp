@@ -1,8 +1,12 @@
 // Host-side checks of the hand-written step adjoint (voxelyze_gb300/csrc/vx_adjoint.cuh):
-//  1. link_forward / voxel_forward reproduce vx64::link_update / vx64::voxel_update bit for bit;
-//  2. link_adjoint / voxel_adjoint agree with central finite differences of those forwards for a
-//     random linear functional of the outputs, input by input.
-// Prints one line per check: "<name> <worst relative error> <cases>"; exits 1 on a forward mismatch.
+//  1. link_forward / voxel_forward reproduce vx64::link_update / vx64::voxel_update bit for bit
+//     (links small- and large-angle, with and without Poisson's ratio or a failure strain; voxels
+//     with and without partial fixes);
+//  2. link_adjoint / voxel_adjoint agree with central finite differences of those forwards, output
+//     by output, input by input (the large-angle links in a check of their own, "link_large");
+//  3. poisson_adjoint agrees with differences of vx64::poisson_strain_links over its links' strains.
+// Prints one line per check: "<name> <worst relative error> <entries> <cases>"; exits 1 on a
+// forward mismatch.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
